@@ -1,0 +1,168 @@
+/*
+ * wpf.h -- C ABI of the GB300-native wPFAW3D time step (libwpf_gb300.so).
+ *
+ * The reference (hfuki/mizuho_edit, wPFAW3D.f90) runs its time step as
+ * argument-less module subroutines over module-global Fortran arrays
+ * (wPFAW3D.f90:95-103, called from program main at :2249-2280).  This header
+ * is the drop-in boundary for that path: the host keeps the driver (config,
+ * time loop, output) and the device owns every field between wpf_upload()
+ * and wpf_download().  One entry point exists per reference routine, plus a
+ * fused wpf_step() that performs the whole loop body with fused kernels.
+ *
+ * Conventions
+ *   - Every function returns an int status, WPF_OK (0) on success.
+ *   - Host arrays are borrowed for the duration of a call only.
+ *   - Field arrays use the reference layout exactly: one-cell halo, Fortran
+ *     order (x fastest), G = (nx+2)*(ny+2)*(nz+2) float64 values, so
+ *     element (i,j,k) with 0 <= i <= nx+1 ... is at i + (nx+2)*(j + (ny+2)*k).
+ *     permeab is (0:3, G) with the component fastest, velocity is (1:3, G).
+ *   - One handle per host thread; all device work of a handle is ordered on
+ *     the handle's CUDA stream, and calls return after that work finishes.
+ *   - There is no CPU fallback: without a usable CUDA device wpf_create()
+ *     fails with WPF_ERR_CUDA.
+ */
+#ifndef WPF_H
+#define WPF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define WPF_OK                 0
+#define WPF_ERR_ARG            1   /* invalid argument or state                    */
+#define WPF_ERR_CUDA           2   /* CUDA runtime error / no device               */
+#define WPF_ERR_NOT_CONVERGED  3   /* solve hit maxit; the best iterate is kept     */
+#define WPF_ERR_NONFINITE      4   /* NaN/Inf in a residual or a reduction         */
+#define WPF_ERR_TIMEOUT        5   /* a bounded device wait expired                */
+#define WPF_ERR_NOMEM          6   /* device allocation failed                     */
+#define WPF_ERR_SINGULAR       7   /* no Dirichlet cell: the Darcy system is singular */
+
+/* ---- solver modes ------------------------------------------------------ */
+#define WPF_SOLVER_FP64   0   /* plain FP64 MG-PCG (the drop-in form)                     */
+#define WPF_SOLVER_MIXED  1   /* FP32 MG-PCG inside FP64 iterative refinement             */
+
+typedef struct wpf_handle wpf_handle;
+
+/* Scalars of Param_type that the step uses (wPFAW3D.f90:27-76). */
+typedef struct wpf_params {
+    int32_t nx, ny, nz;        /* interior grid (single domain)                       */
+    int32_t ix_ref, iy_ref, iz_ref;  /* reference cell of showProgress / getPressure  */
+    double dx;                 /* dxw * epsilon                                        */
+    double epsilon;            /* interface width w (also the anisotropy strength)     */
+    double lambda;             /* phase-concentration coupling                         */
+    double porosity;
+    double viscosity;
+    double diffusion;          /* D                                                    */
+    double ral, rat;           /* dispersivities                                       */
+    double permeab_hole;       /* kwh                                                  */
+    double alpha;              /* 0.5 / b / kc                                         */
+    double tfac;               /* time-step factor of the dt law                       */
+} wpf_params;
+
+/* Well_type (wPFAW3D.f90:82-90): ix/iy/iz are global 1-based indices. */
+typedef struct wpf_well {
+    int32_t ix, iy, iz, pad;
+    double pressure;           /* Dirichlet iff != 0 (wPFAW3D.f90:1106)                */
+    double injection;          /* inlet iff != 0 (wPFAW3D.f90:1140)                    */
+    double phase, concent;     /* fixed values (applied by the host at load time)      */
+} wpf_well;
+
+/* Darcy solver options. */
+typedef struct wpf_solver_opts {
+    int32_t mode;              /* WPF_SOLVER_FP64 or WPF_SOLVER_MIXED                   */
+    int32_t max_outer;         /* FP64 refinement passes (default 20)                  */
+    int32_t max_inner;         /* PCG iterations per pass (default 500)                */
+    int32_t smooth_sweeps;     /* red-black Gauss-Seidel sweeps per V-cycle side (2)   */
+    double rtol;               /* ||b - A p|| <= rtol * ||b|| (true FP64 residual)      */
+    double inner_rtol;         /* inner PCG reduction per pass in MIXED mode (1e-5)    */
+} wpf_solver_opts;
+
+/* Per-step / per-solve statistics. */
+typedef struct wpf_step_stats {
+    int32_t outer_iterations;  /* FP64 residual evaluations after the first            */
+    int32_t inner_iterations;  /* total PCG iterations                                 */
+    int32_t converged;         /* 1 if rtol was met                                    */
+    int32_t overshoot_cells;   /* cells with |phase| > 1 seen by calcPhaseDeriv (:1425) */
+    double relres;             /* final ||b - A p|| / ||b||                             */
+    double taumin;             /* min relaxation time of this step (:1255)              */
+    double dtime;              /* dt used by this step                                  */
+    double max_courant;        /* max |u| * dt / dx over faces (advection CFL)          */
+    double solve_ms;           /* device time of the Darcy solve                       */
+    double update_ms;          /* device time of the rest of the step                  */
+} wpf_step_stats;
+
+/* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */
+typedef struct wpf_diag {
+    double pv;                 /* dx^3 * poro * 0.5 * sum(1 - phase), interior          */
+    double vcal;               /* dx^3 * (1-poro) * 0.5 * sum(1 + phase), interior      */
+    double rwhmax;             /* max distance of a phase > 0 cell from the ref cell    */
+    double phase_max, phase_min, concent_max, concent_min;   /* over G incl. halo      */
+    double pressure_ref;       /* getPressure(ix_ref, iy_ref, iz_ref) (:2151-2166)      */
+    double inlet_flux;         /* sum of u_x across the faces ix = 1 | 2, times dx^2    */
+} wpf_diag;
+
+/* ---- lifetime ------------------------------------------------------------
+ * wpf_create replaces allocate(...) of loadConfig (wPFAW3D.f90:441-449) with
+ * device allocations; wpf_destroy replaces freeField (:2145-2149).           */
+int wpf_create(const wpf_params* p, wpf_handle** out);
+int wpf_destroy(wpf_handle* h);
+const char* wpf_strerror(int status);
+int wpf_device_bytes(const wpf_handle* h, int64_t* bytes);
+
+/* Well table: builds lw (later wells win, wPFAW3D.f90:451-461) and the
+ * Dirichlet / inlet masks used by solvePressure (:1099-1159).               */
+int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell);
+
+/* Upload / download G-sized halo arrays (any pointer may be NULL to skip).
+ * Upload replaces the module arrays permeab_rock, phase, concent, pressure
+ * (loadConfig :464-496 / loadField :547-554); the halos are refreshed on the
+ * device (updateHalo, :1645-1657) and Dirichlet cells get their well pressure.
+ * Download copies them back (permeab is 4*G, velocity 3*G, as the reference). */
+int wpf_upload(wpf_handle* h, const double* permeab_rock, const double* phase,
+               const double* concent, const double* pressure);
+int wpf_download(wpf_handle* h, double* phase, double* concent, double* pressure,
+                 double* permeab, double* velocity, double* dphasedt, double* dconcentdt);
+
+int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o);
+int wpf_get_solver(const wpf_handle* h, wpf_solver_opts* o);
+
+/* ---- the reference routines, one entry point each ------------------------ */
+int wpf_calc_permeability(wpf_handle* h);                          /* :561-599   */
+int wpf_solve_pressure(wpf_handle* h, wpf_step_stats* st);         /* :603-1160  */
+int wpf_calc_velocity(wpf_handle* h);                              /* :1164-1193 */
+int wpf_calc_phase_deriv(wpf_handle* h, double* taumin,
+                         int32_t* overshoot_cells);                /* :1197-1440 */
+int wpf_calc_concent_deriv(wpf_handle* h);                         /* :1554-1624 */
+int wpf_evolve_phase(wpf_handle* h, double dtime);                 /* :1628-1632 */
+int wpf_evolve_concent(wpf_handle* h, double dtime);               /* :1636-1640 */
+
+/* One pass of the main-loop body (wPFAW3D.f90:2226-2280) with fused kernels:
+ * dt law (:2227-2230; *dtime_inout is the previous dt on entry, this step's on
+ * return), calcPermeability, solvePressure, then one fused kernel for
+ * calcVelocity + calcPhaseDeriv + calcConcentDeriv + evolve + updateHalo.
+ * itime is the 1-based step number.  st may be NULL.                        */
+int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* st);
+
+/* nsteps consecutive steps starting at itime0 (no host sync between steps
+ * unless the solver needs one); *dtime_inout as in wpf_step.               */
+int wpf_run(wpf_handle* h, int32_t itime0, int32_t nsteps, double* dtime_inout,
+            wpf_step_stats* last);
+
+/* Diagnostics of showProgress / getPressure on the device.                  */
+int wpf_reduce(wpf_handle* h, wpf_diag* d);
+
+/* Last taumin on the device (the lagged input of the dt law).               */
+int wpf_get_taumin(const wpf_handle* h, double* taumin);
+
+/* Page-locked host buffers for callers that stream fields every step (the
+ * copies in wpf_upload / wpf_download then run at full link bandwidth).     */
+int wpf_host_alloc(int64_t bytes, void** ptr);
+int wpf_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WPF_H */

@@ -1,0 +1,437 @@
+// wpf_capi.cu -- the extern "C" boundary of libwpf_gb300 (declared in include/wpf.h).
+//
+// Each entry point stands in for one module procedure of wPFAW3D.f90; the
+// handle holds what the reference keeps in module-global arrays
+// (wPFAW3D.f90:78-103), resident in device memory.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "wpf_internal.cuh"
+
+using namespace wpf;
+
+namespace wpf {
+
+int dev_alloc(wpf_handle* h, void** p, size_t bytes) {
+    *p = nullptr;
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return WPF_ERR_NOMEM;
+    }
+    if (cudaMemsetAsync(*p, 0, bytes, h->stream) != cudaSuccess) return WPF_ERR_CUDA;
+    h->bytes += (int64_t)bytes;
+    return WPF_OK;
+}
+
+int ensure_per_routine_arrays(wpf_handle* h) {
+    if (h->K0) return WPF_OK;
+    const size_t b = sizeof(double) * h->g.total;
+    double** arrs[9] = {&h->K0, &h->Kf[0], &h->Kf[1], &h->Kf[2], &h->vel[0], &h->vel[1], &h->vel[2],
+                        &h->dphasedt, &h->dconcentdt};
+    for (auto a : arrs) {
+        int rc = dev_alloc(h, (void**)a, b);
+        if (rc) return rc;
+    }
+    return WPF_OK;
+}
+
+}  // namespace wpf
+
+static Phys make_phys(const wpf_params& p) {
+    Phys P;
+    P.dx = p.dx;
+    P.inv_dx = 1.0 / p.dx;
+    P.inv_2dx = 1.0 / (2.0 * p.dx);
+    P.inv_dx2 = 1.0 / (p.dx * p.dx);
+    P.inv_4dx2 = 1.0 / (4.0 * (p.dx * p.dx));
+    P.epsilon = p.epsilon;
+    P.lambda = p.lambda;
+    P.alpha = p.alpha;
+    P.diffusion = p.diffusion;
+    P.ral = p.ral;
+    P.rat = p.rat;
+    P.kwh = p.permeab_hole;
+    P.viscosity = p.viscosity;
+    P.tau_num = 5.0 / 3.0 * p.alpha * p.lambda * (p.epsilon * p.epsilon);   // :1254
+    P.tau0 = P.tau_num / p.diffusion;
+    P.w0 = 2.0 * p.dx;                                                      // :1221
+    P.maxdphi = 2.0 / (2.0 * p.dx);                                          // :1225
+    P.qscale = p.dx * p.dx / (p.dx * p.dx * p.dx);                           // :817
+    return P;
+}
+
+static void free_all(wpf_handle* h) {
+    double* d[] = {h->krock, h->phase, h->concent, h->pressure, h->phase_n, h->concent_n,
+                   h->T[0], h->T[1], h->T[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
+                   h->vel[0], h->vel[1], h->vel[2], h->dphasedt, h->dconcentdt, h->dir_val,
+                   h->qterm, h->dsc, h->partials};
+    for (double* p : d)
+        if (p) cudaFree(p);
+    if (h->flags) cudaFree(h->flags);
+    if (h->dir_idx) cudaFree(h->dir_idx);
+    solver_free(h);
+    if (h->hsc) cudaFreeHost(h->hsc);
+    for (int e = 0; e < 4; ++e)
+        if (h->ev[e]) cudaEventDestroy(h->ev[e]);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+extern "C" {
+
+const char* wpf_strerror(int s) {
+    switch (s) {
+        case WPF_OK: return "ok";
+        case WPF_ERR_ARG: return "invalid argument";
+        case WPF_ERR_CUDA: return "CUDA error (no usable device or a failed launch)";
+        case WPF_ERR_NOT_CONVERGED: return "Darcy solve did not reach the tolerance";
+        case WPF_ERR_NONFINITE: return "non-finite value in a residual or reduction";
+        case WPF_ERR_TIMEOUT: return "bounded device wait expired";
+        case WPF_ERR_NOMEM: return "device allocation failed";
+        case WPF_ERR_SINGULAR: return "no Dirichlet cell: the Darcy system is singular";
+        default: return "unknown status";
+    }
+}
+
+int wpf_create(const wpf_params* p, wpf_handle** out) {
+    if (!p || !out) return WPF_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 1 || p->ny < 1 || p->nz < 1 || !(p->dx > 0) || !(p->viscosity != 0) ||
+        !(p->diffusion != 0) || !(p->epsilon != 0))
+        return WPF_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return WPF_ERR_CUDA;
+    }
+    wpf_handle* h = (wpf_handle*)calloc(1, sizeof(wpf_handle));
+    if (!h) return WPF_ERR_NOMEM;
+    new (&h->h64) Hierarchy<double>();
+    new (&h->h32) Hierarchy<float>();
+    h->prm = *p;
+    h->phys = make_phys(*p);
+    h->g = make_grid(p->nx, p->ny, p->nz);
+    cudaGetDevice(&h->device);
+    int rc = WPF_OK;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) rc = WPF_ERR_CUDA;
+    for (int e = 0; e < 4 && !rc; ++e)
+        if (cudaEventCreate(&h->ev[e]) != cudaSuccess) rc = WPF_ERR_CUDA;
+    if (!rc && cudaMallocHost((void**)&h->hsc, S_COUNT * sizeof(double)) != cudaSuccess)
+        rc = WPF_ERR_CUDA;
+    const size_t fb = sizeof(double) * h->g.total;
+    double** arrs[9] = {&h->krock, &h->phase, &h->concent, &h->pressure, &h->phase_n, &h->concent_n,
+                        &h->T[0], &h->T[1], &h->T[2]};
+    for (int a = 0; a < 9 && !rc; ++a) rc = dev_alloc(h, (void**)arrs[a], fb);
+    if (!rc) rc = dev_alloc(h, (void**)&h->flags, h->g.total);
+    if (!rc) rc = dev_alloc(h, (void**)&h->dsc, S_COUNT * sizeof(double));
+    h->opts.mode = WPF_SOLVER_FP64;
+    h->opts.max_outer = 20;
+    h->opts.max_inner = 500;
+    h->opts.smooth_sweeps = 2;
+    h->opts.rtol = 1e-8;
+    h->opts.inner_rtol = 1e-4;
+    h->taumin_last = 1.0e6;
+    if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = WPF_ERR_CUDA;
+    if (rc) {
+        free_all(h);
+        free(h);
+        return rc;
+    }
+    *out = h;
+    return WPF_OK;
+}
+
+int wpf_destroy(wpf_handle* h) {
+    if (!h) return WPF_ERR_ARG;
+    cudaStreamSynchronize(h->stream);
+    free_all(h);
+    h->h64.~Hierarchy<double>();
+    h->h32.~Hierarchy<float>();
+    free(h);
+    return WPF_OK;
+}
+
+int wpf_device_bytes(const wpf_handle* h, int64_t* bytes) {
+    if (!h || !bytes) return WPF_ERR_ARG;
+    *bytes = h->bytes;
+    return WPF_OK;
+}
+
+int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o) {
+    if (!h || !o) return WPF_ERR_ARG;
+    if (o->mode != WPF_SOLVER_FP64 && o->mode != WPF_SOLVER_MIXED) return WPF_ERR_ARG;
+    if (o->max_outer < 0 || o->max_inner < 1 || !(o->rtol > 0) || o->smooth_sweeps < 0 ||
+        o->smooth_sweeps > 16)
+        return WPF_ERR_ARG;
+    h->opts = *o;
+    if (!(h->opts.inner_rtol > 0 && h->opts.inner_rtol < 1)) h->opts.inner_rtol = 1e-4;
+    if (h->opts.smooth_sweeps == 0) h->opts.smooth_sweeps = 2;
+    return WPF_OK;
+}
+
+int wpf_get_solver(const wpf_handle* h, wpf_solver_opts* o) {
+    if (!h || !o) return WPF_ERR_ARG;
+    *o = h->opts;
+    return WPF_OK;
+}
+
+int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
+    if (!h || nwell < 0 || (nwell > 0 && !wells)) return WPF_ERR_ARG;
+    const Grid& g = h->g;
+    const long long nxh = g.nx + 2, nyh = g.ny + 2, nzh = g.nz + 2;
+    std::vector<int32_t> lw((size_t)(nxh * nyh * nzh), 0);
+    for (int iw = 0; iw < nwell; ++iw) {   // wPFAW3D.f90:453-461 (later wells win)
+        const wpf_well& w = wells[iw];
+        if (0 <= w.ix && w.ix <= g.nx + 1 && 0 <= w.iy && w.iy <= g.ny + 1 && 0 <= w.iz &&
+            w.iz <= g.nz + 1)
+            lw[(size_t)(w.ix + nxh * (w.iy + nyh * w.iz))] = iw + 1;
+    }
+    std::vector<uint8_t> fl((size_t)g.total, 0);
+    std::vector<long long> didx;
+    std::vector<double> dval;
+    std::vector<std::pair<long long, double>> inl;
+    for (int k = 0; k <= g.nz + 1; ++k)
+        for (int j = 0; j <= g.ny + 1; ++j)
+            for (int i = 0; i <= g.nx + 1; ++i) {
+                const int iw = lw[(size_t)(i + nxh * (j + nyh * k))];
+                if (iw <= 0) continue;
+                const wpf_well& w = wells[iw - 1];
+                const long long n = g.at(i, j, k);
+                uint8_t f = F_WELL;
+                const bool interior = i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz;
+                if (w.pressure != 0.0) {
+                    f |= F_DIR;
+                    if (interior) { didx.push_back(n); dval.push_back(w.pressure); }
+                } else if (w.injection != 0.0) {
+                    f |= F_INLET;
+                    if (interior) inl.push_back({n, w.injection});
+                }
+                fl[(size_t)n] = f;
+            }
+    if (h->dir_idx) { cudaFree(h->dir_idx); h->dir_idx = nullptr; }
+    if (h->dir_val) { cudaFree(h->dir_val); h->dir_val = nullptr; }
+    if (h->qterm) { cudaFree(h->qterm); h->qterm = nullptr; }
+    h->ndir = (int32_t)didx.size();
+    h->ninlet = (int32_t)inl.size();
+    int rc;
+    if (h->ndir) {
+        if ((rc = dev_alloc(h, (void**)&h->dir_idx, sizeof(long long) * h->ndir))) return rc;
+        if ((rc = dev_alloc(h, (void**)&h->dir_val, sizeof(double) * h->ndir))) return rc;
+        WPF_CUDA(cudaMemcpyAsync(h->dir_idx, didx.data(), sizeof(long long) * h->ndir,
+                                 cudaMemcpyHostToDevice, h->stream));
+        WPF_CUDA(cudaMemcpyAsync(h->dir_val, dval.data(), sizeof(double) * h->ndir,
+                                 cudaMemcpyHostToDevice, h->stream));
+    }
+    if (h->ninlet) {
+        std::vector<double> q((size_t)g.total, 0.0);
+        for (auto& e : inl) q[(size_t)e.first] = e.second * h->phys.qscale;   // -b of :817
+        if ((rc = dev_alloc(h, (void**)&h->qterm, sizeof(double) * g.total))) return rc;
+        WPF_CUDA(cudaMemcpyAsync(h->qterm, q.data(), sizeof(double) * g.total, cudaMemcpyHostToDevice,
+                                 h->stream));
+    }
+    WPF_CUDA(cudaMemcpyAsync(h->flags, fl.data(), g.total, cudaMemcpyHostToDevice, h->stream));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));   // host vectors go out of scope
+    h->have_wells = true;
+    return phys_set_dirichlet(h);
+}
+
+static int copy_field_in(wpf_handle* h, double* dst, const double* src) {
+    const Grid& g = h->g;
+    WPF_CUDA(cudaMemcpy2DAsync(dst + g.at(0, 0, 0), g.P * sizeof(double), src,
+                               (g.nx + 2) * sizeof(double), (g.nx + 2) * sizeof(double),
+                               (size_t)(g.ny + 2) * (g.nz + 2), cudaMemcpyHostToDevice, h->stream));
+    return WPF_OK;
+}
+
+static int copy_field_out(wpf_handle* h, double* dst, const double* src) {
+    const Grid& g = h->g;
+    WPF_CUDA(cudaMemcpy2DAsync(dst, (g.nx + 2) * sizeof(double), src + g.at(0, 0, 0),
+                               g.P * sizeof(double), (g.nx + 2) * sizeof(double),
+                               (size_t)(g.ny + 2) * (g.nz + 2), cudaMemcpyDeviceToHost, h->stream));
+    return WPF_OK;
+}
+
+int wpf_upload(wpf_handle* h, const double* krock, const double* phase, const double* concent,
+               const double* pressure) {
+    if (!h) return WPF_ERR_ARG;
+    int rc;
+    if (krock) { if ((rc = copy_field_in(h, h->krock, krock))) return rc; if ((rc = phys_halo(h, h->krock))) return rc; }
+    if (phase) { if ((rc = copy_field_in(h, h->phase, phase))) return rc; if ((rc = phys_halo(h, h->phase))) return rc; }
+    if (concent) { if ((rc = copy_field_in(h, h->concent, concent))) return rc; if ((rc = phys_halo(h, h->concent))) return rc; }
+    if (pressure) {
+        if ((rc = copy_field_in(h, h->pressure, pressure))) return rc;
+        if ((rc = phys_set_dirichlet(h))) return rc;
+    }
+    h->vel_valid = false;
+    if (phase || krock) h->kf_valid = false;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_download(wpf_handle* h, double* phase, double* concent, double* pressure, double* permeab,
+                 double* velocity, double* dphasedt, double* dconcentdt) {
+    if (!h) return WPF_ERR_ARG;
+    int rc;
+    if (phase && (rc = copy_field_out(h, phase, h->phase))) return rc;
+    if (concent && (rc = copy_field_out(h, concent, h->concent))) return rc;
+    if (pressure && (rc = copy_field_out(h, pressure, h->pressure))) return rc;
+    if (dphasedt || dconcentdt || permeab || velocity) {
+        if ((rc = ensure_per_routine_arrays(h))) return rc;
+    }
+    if (dphasedt && (rc = copy_field_out(h, dphasedt, h->dphasedt))) return rc;
+    if (dconcentdt && (rc = copy_field_out(h, dconcentdt, h->dconcentdt))) return rc;
+    const Grid& g = h->g;
+    const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    if (permeab || velocity) {
+        std::vector<double> tmp(G);
+        if (permeab) {
+            double* comp[4] = {h->K0, h->Kf[0], h->Kf[1], h->Kf[2]};
+            for (int m = 0; m < 4; ++m) {
+                if ((rc = copy_field_out(h, tmp.data(), comp[m]))) return rc;
+                WPF_CUDA(cudaStreamSynchronize(h->stream));
+                for (size_t n = 0; n < G; ++n) permeab[4 * n + m] = tmp[n];
+            }
+        }
+        if (velocity) {
+            for (int m = 0; m < 3; ++m) {
+                if ((rc = copy_field_out(h, tmp.data(), h->vel[m]))) return rc;
+                WPF_CUDA(cudaStreamSynchronize(h->stream));
+                for (size_t n = 0; n < G; ++n) velocity[3 * n + m] = tmp[n];
+            }
+        }
+    }
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_calc_permeability(wpf_handle* h) {
+    if (!h) return WPF_ERR_ARG;
+    int rc = phys_permeability(h, true);
+    if (rc) return rc;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_solve_pressure(wpf_handle* h, wpf_step_stats* st) {
+    if (!h || !h->have_wells) return WPF_ERR_ARG;
+    wpf_step_stats tmp;
+    memset(&tmp, 0, sizeof(tmp));
+    int rc = solve_pressure(h, st ? st : &tmp);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess && !rc) rc = WPF_ERR_CUDA;
+    return rc;
+}
+
+int wpf_calc_velocity(wpf_handle* h) {
+    if (!h) return WPF_ERR_ARG;
+    int rc = phys_velocity(h);
+    if (rc) return rc;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_calc_phase_deriv(wpf_handle* h, double* taumin, int32_t* overshoot) {
+    if (!h || !h->have_wells) return WPF_ERR_ARG;
+    if (!h->vel_valid) return WPF_ERR_ARG;   // calcVelocity must run first (:2251-2252)
+    return phys_phase_deriv(h, taumin, overshoot);
+}
+
+int wpf_calc_concent_deriv(wpf_handle* h) {
+    if (!h || !h->have_wells || !h->vel_valid) return WPF_ERR_ARG;
+    int rc = phys_concent_deriv(h);
+    if (rc) return rc;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_evolve_phase(wpf_handle* h, double dtime) {
+    if (!h) return WPF_ERR_ARG;
+    int rc = phys_evolve(h, true, dtime);
+    if (rc) return rc;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_evolve_concent(wpf_handle* h, double dtime) {
+    if (!h) return WPF_ERR_ARG;
+    int rc = phys_evolve(h, false, dtime);
+    if (rc) return rc;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
+int wpf_get_taumin(const wpf_handle* h, double* taumin) {
+    if (!h || !taumin) return WPF_ERR_ARG;
+    *taumin = h->taumin_last;
+    return WPF_OK;
+}
+
+int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* st) {
+    if (!h || !dtime_inout || !h->have_wells) return WPF_ERR_ARG;
+    double dt = *dtime_inout;
+    const wpf_params& p = h->prm;
+    if (itime >= 3) {   // wPFAW3D.f90:2227-2230, taumin from the previous step
+        const double e2 = p.epsilon * p.epsilon;
+        const double a = e2 / p.diffusion;
+        dt = p.tfac * 0.5 * (p.dx * p.dx) / e2 * (a < h->taumin_last ? a : h->taumin_last);
+    }
+    wpf_step_stats tmp;
+    memset(&tmp, 0, sizeof(tmp));
+    wpf_step_stats* s = st ? st : &tmp;
+    int rc = phys_permeability(h, false);
+    if (rc) return rc;
+    const int srs = solve_pressure(h, s);
+    if (srs && srs != WPF_ERR_NOT_CONVERGED) return srs;
+    WPF_CUDA(cudaEventRecord(h->ev[2], h->stream));
+    double taumin = 0, umax = 0;
+    int32_t over = 0;
+    rc = phys_fused_update(h, dt, &taumin, &over, &umax);
+    if (rc) return rc;
+    WPF_CUDA(cudaEventRecord(h->ev[3], h->stream));
+    WPF_CUDA(cudaEventSynchronize(h->ev[3]));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+    s->update_ms = ms;
+    s->taumin = taumin;
+    s->overshoot_cells = over;
+    s->dtime = dt;
+    s->max_courant = umax * dt / p.dx;
+    *dtime_inout = dt;
+    return srs;
+}
+
+int wpf_run(wpf_handle* h, int32_t itime0, int32_t nsteps, double* dtime_inout,
+            wpf_step_stats* last) {
+    if (!h || nsteps < 0 || !dtime_inout) return WPF_ERR_ARG;
+    int rc = WPF_OK;
+    for (int s = 0; s < nsteps; ++s) {
+        rc = wpf_step(h, itime0 + s, dtime_inout, last);
+        if (rc && rc != WPF_ERR_NOT_CONVERGED) return rc;
+    }
+    return rc;
+}
+
+int wpf_host_alloc(int64_t bytes, void** ptr) {
+    if (!ptr || bytes <= 0) return WPF_ERR_ARG;
+    if (cudaMallocHost(ptr, (size_t)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return WPF_ERR_NOMEM;
+    }
+    return WPF_OK;
+}
+
+int wpf_host_free(void* ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) return WPF_ERR_CUDA;
+    return WPF_OK;
+}
+
+int wpf_reduce(wpf_handle* h, wpf_diag* d) {
+    if (!h || !d) return WPF_ERR_ARG;
+    return phys_reduce(h, d);
+}
+
+}  // extern "C"

@@ -1,0 +1,638 @@
+// wpf_physics.cu -- FP64 field kernels of the wPFAW3D step on sm_103a.
+//
+// Per-cell physics follows wPFAW3D.f90 (calcPermeability :561-599,
+// calcVelocity :1164-1193, calcPhaseDeriv :1197-1440, calcConcentDeriv
+// :1554-1624, evolve* :1628-1640, updateHalo :1645-1657).  The trigonometric
+// functions of calcPhaseDeriv are replaced by exact identities:
+//   theta = atan(t), t = phiy/a, a = phix + 1e-20:
+//     cos^2 = a^2/(a^2+phiy^2), sin^2 = phiy^2/(a^2+phiy^2),
+//     cos = |a|/sqrt(a^2+phiy^2), sin = sign(a)*phiy/sqrt(a^2+phiy^2);
+//   phi = acos(u), u = phiz/(|grad phi| + 1e-20):
+//     cos 4phi = 8u^2(u^2-1)+1, sin 4phi = 4u sqrt(1-u^2)(2u^2-1),
+//   cos 2theta = cos^2 - sin^2.
+// and the angular-derivative terms f2, f4, f5, f6 are exactly zero unless one
+// of the signed guards phix, phiy, phiz > 1/dx (:1333, :1342, :1355) holds,
+// which needs a phase overshoot; the kernel evaluates them only then.
+//
+// FP64 on GB300 issues at a small fraction of the FP32 rate, so the kernels
+// replace divisions by precomputed reciprocals where the reference divides by
+// a parameter (dx, mu); results differ from the literal Fortran arithmetic by
+// a few ulp, well inside the parity tolerances.
+#include "wpf_internal.cuh"
+
+namespace wpf {
+
+// ---------------------------------------------------------------------------
+// per-cell device functions shared by the per-routine and fused kernels
+// ---------------------------------------------------------------------------
+
+// dphasedt and tau of one interior cell (calcPhaseDeriv, wPFAW3D.f90:1231-1414).
+// ph points at the phase field, n is the cell, sy/sz the y/z strides.
+// v{x,y,z}{p,m} are the six face velocities around the cell.
+__device__ __forceinline__ void phase_cell(const double* __restrict__ ph, long long n, long long sy,
+                                           long long sz, double vxp, double vxm, double vyp,
+                                           double vym, double vzp, double vzm, double conc,
+                                           bool well, const Phys& P, double& rate, double& tau,
+                                           int& over) {
+    const double c0 = ph[n];
+    const double pe = ph[n + 1], pw = ph[n - 1], pn = ph[n + sy], ps = ph[n - sy];
+    const double pt = ph[n + sz], pb = ph[n - sz];
+    const double phix = (pe - pw) * P.inv_2dx;       // grad_phase, :1472-1474
+    const double phiy = (pn - ps) * P.inv_2dx;
+    const double phiz = (pt - pb) * P.inv_2dx;
+    const double dpf = sqrt(phix * phix + phiy * phiy + phiz * phiz);   // :1232
+    double vs = 0.0;
+    if (dpf > 1.0e-6) {                                                  // :1234-1244
+        const double vx = 0.5 * (vxp + vxm), vy = 0.5 * (vyp + vym), vz = 0.5 * (vzp + vzm);
+        vs = (vx * phix + vy * phiy + vz * phiz) / dpf;
+    }
+    tau = P.tau0;                                                        // :1246-1254
+    if (!(vs >= 0.0)) {
+        const double kxx = P.diffusion + fabs(conc) * P.epsilon * (P.ral * (vs * vs)) / sqrt(vs * vs);
+        tau = P.tau_num / kxx;
+    }
+    over = 0;
+    rate = 0.0;
+    if (well) return;                                                    // :1257-1261
+    if (phix == 0.0 && phiy == 0.0 && phiz == 0.0) {                     // :1283-1286
+        const double pxx = pe - 2.0 * c0 + pw, pyy = pn - 2.0 * c0 + ps, pzz = pt - 2.0 * c0 + pb;
+        const double pxy = ph[n + 1 + sy] - ph[n + 1 - sy] - ph[n - 1 + sy] + ph[n - 1 - sy];
+        const double pyz = ph[n + sy + sz] - ph[n - sy + sz] - ph[n + sy - sz] + ph[n - sy - sz];
+        const double pzx = ph[n + 1 + sz] - ph[n - 1 + sz] - ph[n + 1 - sz] + ph[n - 1 - sz];
+        if (pxx == 0.0 && pyy == 0.0 && pzz == 0.0 && pxy == 0.0 && pyz == 0.0 && pzx == 0.0) return;
+    }
+    const double lap = (pe + pw + pn + ps + pt + pb - 6.0 * c0) * P.inv_dx2;   // :1451-1460
+    const double f1 = (1.0 - c0 * c0) * (c0 - P.lambda * conc);                // :1381
+    const double a = phix + 1.0e-20;
+    const double a2 = a * a, py2 = phiy * phiy;
+    const double dd = dpf + 1.0e-20;
+    const bool gth = phix > P.maxdphi || phiy > P.maxdphi;                       // :1333, :1355
+    const bool gph = gth || phiz > P.maxdphi;                                    // :1342
+    if (!gph) {
+        // f2 = f4 = f5 = f6 = 0: only W (:1309) is needed.
+        const double inv = 1.0 / (a2 + py2);
+        const double c2 = a2 * inv, s2 = py2 * inv;
+        const double u2 = (phiz * phiz) / (dd * dd);
+        const double c4phi = 8.0 * u2 * (u2 - 1.0) + 1.0;
+        const double w = P.w0 * (1.0 + P.epsilon * (7.0 * (c2 * c2) - 6.0 * c2 + (s2 * s2) * c4phi));
+        rate = (f1 + (w * w) * lap) / tau;
+    } else {
+        const double rn = 1.0 / sqrt(a2 + py2);
+        const double c = fabs(a) * rn;
+        const double s = copysign(1.0, a) * phiy * rn;
+        double u = phiz / dd;
+        u = fmin(1.0, fmax(-1.0, u));
+        const double u2 = u * u;
+        const double sp = sqrt(fmax(0.0, 1.0 - u2));
+        const double c4phi = 8.0 * u2 * (u2 - 1.0) + 1.0;
+        const double s4phi = 4.0 * u * sp * (2.0 * u2 - 1.0);
+        const double c2 = c * c, s2 = s * s, c4 = c2 * c2, s4 = s2 * s2;
+        const double cos2t = c2 - s2;
+        const double eps = P.epsilon, w0 = P.w0;
+        const double w = w0 * (1.0 + eps * (7.0 * c4 - 6.0 * c2 + s4 * c4phi));                 // :1309
+        const double dwdth = w0 * (4.0 * eps * s * c * (-7.0 * c2 + 3.0 + s2 * c4phi));        // :1312
+        const double ddwdth = w0 * (4.0 * eps * (cos2t * (-7.0 * c2 + 3.0 + s2 * c4phi) +
+                                                 2.0 * s2 * c2 * (7.0 + c4phi)));               // :1316
+        const double dwdph = w0 * (-4.0 * eps * s4 * s4phi);                                    // :1320
+        const double ddwdph = w0 * (-16.0 * eps * s4 * c4phi);                                  // :1323
+        const double ddwdthph = w0 * (-16.0 * eps * (s2 * s) * c * s4phi);                      // :1326
+        const double pxx = (pe - 2.0 * c0 + pw) * P.inv_dx2;
+        const double pyy = (pn - 2.0 * c0 + ps) * P.inv_dx2;
+        const double pzz = (pt - 2.0 * c0 + pb) * P.inv_dx2;
+        const double pxy = (ph[n + 1 + sy] - ph[n + 1 - sy] - ph[n - 1 + sy] + ph[n - 1 - sy]) * P.inv_4dx2;
+        const double pyz = (ph[n + sy + sz] - ph[n - sy + sz] - ph[n + sy - sz] + ph[n - sy - sz]) * P.inv_4dx2;
+        const double pzx = (ph[n + 1 + sz] - ph[n - 1 + sz] - ph[n + 1 - sz] + ph[n - 1 - sz]) * P.inv_4dx2;
+        const double rxy2 = phix * phix + phiy * phiy;
+        const double r2 = rxy2 + phiz * phiz;
+        double dthx = 0.0, dthy = 0.0, dthz = 0.0, dthpx = 0.0, dthpy = 0.0;
+        if (gth) {                                                                              // :1333-1337
+            const double den = 1.0 / (rxy2 + 1.0e-20);
+            dthx = (pxy * phix - phiy * pxx) * den;
+            dthy = (pyy * phix - phiy * pxy) * den;
+            dthz = (pyz * phix - phiy * pzx) * den;
+            dthpx = -phiy * r2 * den;                                                           // :1356
+            dthpy = phix * r2 * den;                                                            // :1357
+        }
+        const double rxy = sqrt(rxy2);
+        const double den2 = 1.0 / (r2 * rxy + 1.0e-20);                                         // :1344
+        const double dphx = (phiz * (phix * pxx + phiy * pxy) - rxy2 * pzx) * den2;
+        const double dphy = (phiz * (phix * pxy + phiy * pyy) - rxy2 * pyz) * den2;
+        const double dphz = (phiz * (phix * pzx + phiy * pyz) - rxy2 * pzz) * den2;
+        const double dphpx = phix * phiz / (rxy * dpf + 1.0e-20);                               // :1363
+        const double dphpy = phiy * phiz / (rxy * dpf + 1.0e-20);                               // :1364
+        const double dphpz = -rxy / dd;                                                         // :1365
+        const double dwdx = dwdth * dthx + dwdph * dphx;                                        // :1367
+        const double dwdy = dwdth * dthy + dwdph * dphy;
+        const double dwdz = dwdth * dthz + dwdph * dphz;
+        const double ddwthx = ddwdth * dthx + ddwdthph * dphx;                                  // :1371
+        const double ddwthy = ddwdth * dthy + ddwdthph * dphy;
+        const double ddwthz = ddwdth * dthz + ddwdthph * dphz;
+        const double ddwphx = ddwdph * dphx + ddwdthph * dthx;                                  // :1375
+        const double ddwphy = ddwdph * dphy + ddwdthph * dthy;
+        const double ddwphz = ddwdph * dphz + ddwdthph * dthz;
+        const double d2 = dpf * dpf;
+        const double f2 = 2.0 * w * (dwdx * phix + dwdy * phiy + dwdz * phiz);                  // :1386
+        const double f3 = (w * w) * lap;                                                        // :1390
+        const double f4 = dwdx * (dwdth * dthpx * d2 + dwdph * dphpx * d2) +
+                          w * (ddwthx * dthpx * d2 + ddwphx * dphpx * d2);                      // :1395
+        const double f5 = dwdy * (dwdth * dthpy * d2 + dwdph * dphpy * d2) +
+                          w * (ddwthy * dthpy * d2 + ddwphy * dphpy * d2);                      // :1401
+        const double f6 = dwdz * (dwdph * dphpz * d2) + w * (ddwphz * dphpz * d2);              // :1407
+        (void)ddwthz;
+        rate = (f1 + f2 + f3 + f4 + f5 + f6) / tau;                                             // :1414
+    }
+    over = (c0 > 1.0 || c0 < -1.0) ? 1 : 0;                                                     // :1425
+}
+
+// dconcentdt of one non-well interior cell (calcConcentDeriv, :1568-1606).
+__device__ __forceinline__ double concent_cell(const double* __restrict__ C, long long n,
+                                               long long sy, long long sz, double uxp, double uxm,
+                                               double uyp, double uym, double uzp, double uzm,
+                                               double dphidt, const Phys& P) {
+    const double c0 = C[n];
+    const double ce = C[n + 1], cw = C[n - 1], cn = C[n + sy], cs = C[n - sy];
+    const double ct = C[n + sz], cb = C[n - sz];
+    const double lap = (ce + cw + cn + cs + ct + cb - 6.0 * c0) * P.inv_dx2;
+    const double fxp = uxp * (uxp > 0.0 ? c0 : ce), fxm = uxm * (uxm > 0.0 ? cw : c0);
+    const double fyp = uyp * (uyp > 0.0 ? c0 : cn), fym = uym * (uym > 0.0 ? cs : c0);
+    const double fzp = uzp * (uzp > 0.0 ? c0 : ct), fzm = uzm * (uzm > 0.0 ? cb : c0);
+    const double div = (fxp - fxm) * P.inv_dx + (fyp - fym) * P.inv_dx + (fzp - fzm) * P.inv_dx;
+    return P.diffusion * lap + P.alpha * dphidt - div;
+}
+
+__device__ __forceinline__ void flush_step_reductions(double tau, int over, double umax, double* dsc) {
+    __shared__ double sm[32];
+    __shared__ int smi[32];
+    const double tmin = block_min(tau, sm, 1.0e308);
+    const int osum = block_sum(over, smi);
+    const double um = block_max(umax, sm, 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        atomicMin(reinterpret_cast<unsigned long long*>(dsc + S_TAUMIN_KEY), dkey(tmin));
+        if (osum) atomicAdd(reinterpret_cast<unsigned long long*>(dsc + S_OVERSHOOT),
+                            (unsigned long long)osum);
+        atomicMax(reinterpret_cast<unsigned long long*>(dsc + S_UMAX_BITS),
+                  (unsigned long long)__double_as_longlong(um));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// calcPermeability (:561-599).  One thread per face-cell (i,j,k) in
+// [0..nx]x[0..ny]x[0..nz]: the cell permeability K0 = kwh f + Krock (1-f) of
+// the cell and its +x/+y/+z neighbours, and the three harmonic means
+// 2ab/(a+b) (= 2/(1/a+1/b)).  T = K_f/mu with the global boundary faces set
+// to zero (the merge guards of :843-848); Kf/K0 only when materialised.
+// ---------------------------------------------------------------------------
+__global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
+                               const double* __restrict__ kr, double* __restrict__ Tx,
+                               double* __restrict__ Ty, double* __restrict__ Tz,
+                               double* __restrict__ Kx, double* __restrict__ Ky,
+                               double* __restrict__ Kz, double inv_mu) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    auto K0 = [&](long long m) {
+        const double f = 0.5 * (1.0 + ph[m]);
+        return P.kwh * f + kr[m] * (1.0 - f);
+    };
+    const double a = K0(n);
+    const double bx = K0(n + 1), by = K0(n + g.P), bz = K0(n + g.S);
+    const double kx = 2.0 * a * bx / (a + bx);
+    const double ky = 2.0 * a * by / (a + by);
+    const double kz = 2.0 * a * bz / (a + bz);
+    const bool in_j = j >= 1 && j <= g.ny, in_k = k >= 1 && k <= g.nz, in_i = i >= 1 && i <= g.nx;
+    Tx[n] = (i >= 1 && i < g.nx && in_j && in_k) ? kx * inv_mu : 0.0;
+    Ty[n] = (j >= 1 && j < g.ny && in_i && in_k) ? ky * inv_mu : 0.0;
+    Tz[n] = (k >= 1 && k < g.nz && in_i && in_j) ? kz * inv_mu : 0.0;
+    if (Kx) { Kx[n] = kx; Ky[n] = ky; Kz[n] = kz; }
+}
+
+// K0 over every cell of the halo grid (:567-574), for downloads only.
+__global__ void k_cell_K0(Grid g, Phys P, const double* __restrict__ ph,
+                          const double* __restrict__ kr, double* __restrict__ K0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx + 1 || j > g.ny + 1 || k > g.nz + 1) return;
+    const long long n = g.at(i, j, k);
+    const double f = 0.5 * (1.0 + ph[n]);
+    K0[n] = P.kwh * f + kr[n] * (1.0 - f);
+}
+
+// calcVelocity (:1169-1176): faces 0..n in every direction, unmasked K_f.
+__global__ void k_velocity(Grid g, Phys P, const double* __restrict__ pr,
+                           const double* __restrict__ Kx, const double* __restrict__ Ky,
+                           const double* __restrict__ Kz, double* __restrict__ vx,
+                           double* __restrict__ vy, double* __restrict__ vz, double inv_mu) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    const double p0 = pr[n];
+    vx[n] = -(Kx[n] * inv_mu * ((pr[n + 1] - p0) * P.inv_dx));
+    vy[n] = -(Ky[n] * inv_mu * ((pr[n + g.P] - p0) * P.inv_dx));
+    vz[n] = -(Kz[n] * inv_mu * ((pr[n + g.S] - p0) * P.inv_dx));
+}
+
+// calcPhaseDeriv over the interior (:1227-1437) from the velocity arrays.
+__global__ void __launch_bounds__(256) k_phase_deriv(Grid g, Phys P, const double* __restrict__ ph,
+                                                     const double* __restrict__ cc,
+                                                     const double* __restrict__ vx,
+                                                     const double* __restrict__ vy,
+                                                     const double* __restrict__ vz,
+                                                     const uint8_t* __restrict__ fl,
+                                                     double* __restrict__ dph, double* dsc) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    double tau = 1.0e308;
+    int over = 0;
+    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+        const long long n = g.at(i, j, k);
+        double rate;
+        phase_cell(ph, n, g.P, g.S, vx[n], vx[n - 1], vy[n], vy[n - g.P], vz[n], vz[n - g.S], cc[n],
+                   (fl[n] & F_WELL) != 0, P, rate, tau, over);
+        dph[n] = rate;
+    }
+    flush_step_reductions(tau, over, 0.0, dsc);
+}
+
+// calcConcentDeriv over the interior (:1559-1576).
+__global__ void k_concent_deriv(Grid g, Phys P, const double* __restrict__ cc,
+                                const double* __restrict__ vx, const double* __restrict__ vy,
+                                const double* __restrict__ vz, const uint8_t* __restrict__ fl,
+                                const double* __restrict__ dph, double* __restrict__ dcc) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    if (fl[n] & F_WELL) { dcc[n] = 0.0; return; }
+    dcc[n] = concent_cell(cc, n, g.P, g.S, vx[n], vx[n - 1], vy[n], vy[n - g.P], vz[n], vz[n - g.S],
+                          dph[n], P);
+}
+
+// Euler update over the interior (the halo derivative is zero, :1629/:1637).
+__global__ void k_evolve(Grid g, double* __restrict__ f, const double* __restrict__ d, double dt) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    f[n] = f[n] + d[n] * dt;
+}
+
+// updateHalo (:1651-1656): the sequential x, y, z plane copies leave every
+// halo cell equal to the interior cell at the clamped index; one thread per
+// halo cell.  Index space: x faces (2*(ny+2)*(nz+2)), y faces (2*nx*(nz+2)),
+// z faces (2*nx*ny).
+__global__ void k_halo(Grid g, double* __restrict__ f) {
+    const long long nxf = 2LL * (g.ny + 2) * (g.nz + 2);
+    const long long nyf = 2LL * g.nx * (g.nz + 2);
+    const long long nzf = 2LL * g.nx * g.ny;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (t < nxf) {
+        const int side = (int)(t & 1); t >>= 1;
+        j = (int)(t % (g.ny + 2)); k = (int)(t / (g.ny + 2));
+        i = side ? g.nx + 1 : 0;
+    } else if ((t -= nxf) < nyf) {
+        const int side = (int)(t & 1); t >>= 1;
+        i = 1 + (int)(t % g.nx); k = (int)(t / g.nx);
+        j = side ? g.ny + 1 : 0;
+    } else if ((t -= nyf) < nzf) {
+        const int side = (int)(t & 1); t >>= 1;
+        i = 1 + (int)(t % g.nx); j = 1 + (int)(t / g.nx);
+        k = side ? g.nz + 1 : 0;
+    } else {
+        return;
+    }
+    const int si = min(max(i, 1), g.nx), sj = min(max(j, 1), g.ny), sk = min(max(k, 1), g.nz);
+    f[g.at(i, j, k)] = f[g.at(si, sj, sk)];
+}
+
+// Write v to every halo cell whose clamped source is the boundary cell (i,j,k).
+__device__ __forceinline__ void write_halo_of(const Grid& g, int i, int j, int k, double* __restrict__ f,
+                                              double v) {
+    const int i0 = i == 1 ? -1 : 0, i1 = i == g.nx ? 1 : 0;
+    const int j0 = j == 1 ? -1 : 0, j1 = j == g.ny ? 1 : 0;
+    const int k0 = k == 1 ? -1 : 0, k1 = k == g.nz ? 1 : 0;
+    if (!(i0 | i1 | j0 | j1 | k0 | k1)) return;
+    for (int dk = k0; dk <= k1; ++dk)
+        for (int dj = j0; dj <= j1; ++dj)
+            for (int di = i0; di <= i1; ++di)
+                if (di | dj | dk) f[g.at(i + di, j + dj, k + dk)] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Fused update: calcVelocity + calcPhaseDeriv + calcConcentDeriv + evolvePhase
+// + evolveConcent + updateHalo for one interior cell per thread.  The face
+// velocities come straight from T = K_f/mu and the solved pressure (zero on
+// the global boundary faces, as the reference's halo copy makes them); the
+// new phase / concentration go to the ping-pong buffers with their halo.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_fused_update(Grid g, Phys P, const double* __restrict__ ph,
+                                                      const double* __restrict__ cc,
+                                                      const double* __restrict__ pr,
+                                                      const double* __restrict__ Tx,
+                                                      const double* __restrict__ Ty,
+                                                      const double* __restrict__ Tz,
+                                                      const uint8_t* __restrict__ fl,
+                                                      double* __restrict__ ph_out,
+                                                      double* __restrict__ cc_out, double dt,
+                                                      double* dsc) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    double tau = 1.0e308, umax = 0.0;
+    int over = 0;
+    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+        const long long n = g.at(i, j, k);
+        const long long sy = g.P, sz = g.S;
+        const double p0 = pr[n];
+        const double uxp = -(Tx[n] * ((pr[n + 1] - p0) * P.inv_dx));
+        const double uxm = -(Tx[n - 1] * ((p0 - pr[n - 1]) * P.inv_dx));
+        const double uyp = -(Ty[n] * ((pr[n + sy] - p0) * P.inv_dx));
+        const double uym = -(Ty[n - sy] * ((p0 - pr[n - sy]) * P.inv_dx));
+        const double uzp = -(Tz[n] * ((pr[n + sz] - p0) * P.inv_dx));
+        const double uzm = -(Tz[n - sz] * ((p0 - pr[n - sz]) * P.inv_dx));
+        const bool well = (fl[n] & F_WELL) != 0;
+        const double conc = cc[n];
+        double rate;
+        phase_cell(ph, n, sy, sz, uxp, uxm, uyp, uym, uzp, uzm, conc, well, P, rate, tau, over);
+        const double crate = well ? 0.0 : concent_cell(cc, n, sy, sz, uxp, uxm, uyp, uym, uzp, uzm,
+                                                       rate, P);
+        const double phn = ph[n] + rate * dt;
+        const double ccn = conc + crate * dt;
+        ph_out[n] = phn;
+        cc_out[n] = ccn;
+        write_halo_of(g, i, j, k, ph_out, phn);
+        write_halo_of(g, i, j, k, cc_out, ccn);
+        umax = fmax(fabs(uxp), fmax(fabs(uyp), fabs(uzp)));
+    }
+    flush_step_reductions(tau, over, umax, dsc);
+}
+
+// Pressure of the Dirichlet cells := well pressure (the identity rows of :840).
+__global__ void k_set_dirichlet(double* __restrict__ pr, const long long* __restrict__ idx,
+                                const double* __restrict__ val, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) pr[idx[t]] = val[t];
+}
+
+// ---------------------------------------------------------------------------
+// showProgress reductions (:1695, :1756-1810): per-block partials of
+//   S0 = sum(1-phase), S1 = sum(1+phase)  (interior, compensated per thread)
+//   M0 = max r^2 over phase > 0, max/min phase, max/min concent (over G)
+//   S2 = inlet flux sum u_x(1->2) dx^2
+// then one block folds the partials in a fixed order.
+// ---------------------------------------------------------------------------
+struct DiagPart {
+    double s0, c0, s1, c1, s2, c2, r2max, pmax, pmin, cmax, cmin;
+};
+
+__device__ __forceinline__ void two_sum(double& s, double& c, double v) {
+    const double t = s + v;
+    const double bp = t - s;
+    c += (s - (t - bp)) + (v - bp);
+    s = t;
+}
+
+__global__ void k_diag_partial(Grid g, Phys P, int ix_ref, int iy_ref, int iz_ref,
+                               const double* __restrict__ ph, const double* __restrict__ cc,
+                               const double* __restrict__ pr, const double* __restrict__ Tx,
+                               DiagPart* __restrict__ out) {
+    // one block per (j,k) plane slab: blockIdx.x = k (0..nz+1), threads over rows j and x
+    __shared__ double sm[32];
+    const int k = blockIdx.x;
+    double s0 = 0, c0 = 0, s1 = 0, c1 = 0, s2 = 0, c2 = 0, r2max = 0;
+    double pmax = -1.0e308, pmin = 1.0e308, cmax = -1.0e308, cmin = 1.0e308;
+    const double dx = P.dx;
+    const double xref = dx * (ix_ref - 1) + 0.5 * dx, yref = dx * (iy_ref - 1) + 0.5 * dx,
+                 zref = dx * (iz_ref - 1) + 0.5 * dx;
+    for (int j = threadIdx.y; j <= g.ny + 1; j += blockDim.y)
+        for (int i = threadIdx.x; i <= g.nx + 1; i += blockDim.x) {
+            const long long n = g.at(i, j, k);
+            const double f = ph[n], c = cc[n];
+            pmax = fmax(pmax, f); pmin = fmin(pmin, f);
+            cmax = fmax(cmax, c); cmin = fmin(cmin, c);
+            const bool interior = i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz;
+            if (interior) {
+                two_sum(s0, c0, 1.0 - f);
+                two_sum(s1, c1, 1.0 + f);
+                if (f > 0.0) {
+                    const double x = dx * (i - 1) + 0.5 * dx - xref, y = dx * (j - 1) + 0.5 * dx - yref,
+                                 z = dx * (k - 1) + 0.5 * dx - zref;
+                    r2max = fmax(r2max, x * x + y * y + z * z);
+                }
+                if (i == 1 && g.nx >= 2) {
+                    const double u = -(Tx[n] * ((pr[n + 1] - pr[n]) * P.inv_dx));
+                    two_sum(s2, c2, u * dx * dx);
+                }
+            }
+        }
+    DiagPart r;
+    r.s0 = block_sum(s0, sm); r.c0 = block_sum(c0, sm);
+    r.s1 = block_sum(s1, sm); r.c1 = block_sum(c1, sm);
+    r.s2 = block_sum(s2, sm); r.c2 = block_sum(c2, sm);
+    r.r2max = block_max(r2max, sm, 0.0);
+    r.pmax = block_max(pmax, sm, -1.0e308); r.pmin = block_min(pmin, sm, 1.0e308);
+    r.cmax = block_max(cmax, sm, -1.0e308); r.cmin = block_min(cmin, sm, 1.0e308);
+    if (threadIdx.x == 0 && threadIdx.y == 0) out[k] = r;
+}
+
+__global__ void k_diag_final(const DiagPart* __restrict__ parts, int nparts, double* out) {
+    if (threadIdx.x != 0) return;
+    double s0 = 0, c0 = 0, s1 = 0, c1 = 0, s2 = 0, c2 = 0, r2 = 0;
+    double pmax = -1.0e308, pmin = 1.0e308, cmax = -1.0e308, cmin = 1.0e308;
+    for (int q = 0; q < nparts; ++q) {
+        const DiagPart& p = parts[q];
+        two_sum(s0, c0, p.s0); c0 += p.c0;
+        two_sum(s1, c1, p.s1); c1 += p.c1;
+        two_sum(s2, c2, p.s2); c2 += p.c2;
+        r2 = fmax(r2, p.r2max);
+        pmax = fmax(pmax, p.pmax); pmin = fmin(pmin, p.pmin);
+        cmax = fmax(cmax, p.cmax); cmin = fmin(cmin, p.cmin);
+    }
+    out[0] = s0 + c0; out[1] = s1 + c1; out[2] = s2 + c2; out[3] = r2;
+    out[4] = pmax; out[5] = pmin; out[6] = cmax; out[7] = cmin;
+}
+
+// ---------------------------------------------------------------------------
+// host wrappers
+// ---------------------------------------------------------------------------
+static void reset_step_slots(wpf_handle* h) {
+    // taumin starts at 1e6 (:1223); overshoot and umax at zero.
+    h->hsc[S_TAUMIN_KEY] = 0;
+    unsigned long long key = dkey_host(1.0e6);
+    unsigned long long zero = 0;
+    memcpy(&h->hsc[S_TAUMIN_KEY], &key, 8);
+    memcpy(&h->hsc[S_OVERSHOOT], &zero, 8);
+    memcpy(&h->hsc[S_UMAX_BITS], &zero, 8);
+}
+
+static int upload_step_slots(wpf_handle* h) {
+    reset_step_slots(h);
+    WPF_CUDA(cudaMemcpyAsync(h->dsc + S_TAUMIN_KEY, h->hsc + S_TAUMIN_KEY, 3 * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream));
+    return WPF_OK;
+}
+
+static int read_step_slots(wpf_handle* h, double* taumin, int32_t* overshoot, double* umax) {
+    WPF_CUDA(cudaMemcpyAsync(h->hsc + S_TAUMIN_KEY, h->dsc + S_TAUMIN_KEY, 3 * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    unsigned long long key, ov, um;
+    memcpy(&key, &h->hsc[S_TAUMIN_KEY], 8);
+    memcpy(&ov, &h->hsc[S_OVERSHOOT], 8);
+    memcpy(&um, &h->hsc[S_UMAX_BITS], 8);
+    const double tm = dkey_inv(key);
+    h->taumin_last = tm;
+    if (taumin) *taumin = tm;
+    if (overshoot) *overshoot = (int32_t)ov;
+    if (umax) { double v; memcpy(&v, &um, 8); *umax = v; }
+    return WPF_OK;
+}
+
+static double inv_mu(const wpf_handle* h) { return 1.0 / h->prm.viscosity; }
+
+int phys_permeability(wpf_handle* h, bool materialise) {
+    const Grid& g = h->g;
+    dim3 b = cell_block(), gr = cell_grid(g.nx + 1, g.ny + 1, g.nz + 1);
+    if (materialise) {
+        int rc = ensure_per_routine_arrays(h);
+        if (rc) return rc;
+        k_cell_K0<<<cell_grid(g.nx + 2, g.ny + 2, g.nz + 2), b, 0, h->stream>>>(g, h->phys, h->phase,
+                                                                               h->krock, h->K0);
+    }
+    k_permeability<<<gr, b, 0, h->stream>>>(g, h->phys, h->phase, h->krock, h->T[0], h->T[1], h->T[2],
+                                            materialise ? h->Kf[0] : nullptr,
+                                            materialise ? h->Kf[1] : nullptr,
+                                            materialise ? h->Kf[2] : nullptr, inv_mu(h));
+    WPF_CUDA(cudaGetLastError());
+    h->kf_valid = materialise;
+    return WPF_OK;
+}
+
+int phys_velocity(wpf_handle* h) {
+    int rc = ensure_per_routine_arrays(h);
+    if (rc) return rc;
+    if (!h->kf_valid) return WPF_ERR_ARG;   // calcPermeability must precede (:2249-2251)
+    const Grid& g = h->g;
+    k_velocity<<<cell_grid(g.nx + 1, g.ny + 1, g.nz + 1), cell_block(), 0, h->stream>>>(
+        g, h->phys, h->pressure, h->Kf[0], h->Kf[1], h->Kf[2], h->vel[0], h->vel[1], h->vel[2],
+        inv_mu(h));
+    WPF_CUDA(cudaGetLastError());
+    h->vel_valid = true;
+    return WPF_OK;
+}
+
+int phys_phase_deriv(wpf_handle* h, double* taumin, int32_t* overshoot) {
+    int rc = ensure_per_routine_arrays(h);
+    if (rc) return rc;
+    const Grid& g = h->g;
+    if ((rc = upload_step_slots(h))) return rc;
+    k_phase_deriv<<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
+        g, h->phys, h->phase, h->concent, h->vel[0], h->vel[1], h->vel[2], h->flags, h->dphasedt,
+        h->dsc);
+    WPF_CUDA(cudaGetLastError());
+    return read_step_slots(h, taumin, overshoot, nullptr);
+}
+
+int phys_concent_deriv(wpf_handle* h) {
+    int rc = ensure_per_routine_arrays(h);
+    if (rc) return rc;
+    const Grid& g = h->g;
+    k_concent_deriv<<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
+        g, h->phys, h->concent, h->vel[0], h->vel[1], h->vel[2], h->flags, h->dphasedt,
+        h->dconcentdt);
+    WPF_CUDA(cudaGetLastError());
+    return WPF_OK;
+}
+
+int phys_halo(wpf_handle* h, double* f) {
+    const Grid& g = h->g;
+    const long long n = 2LL * (g.ny + 2) * (g.nz + 2) + 2LL * g.nx * (g.nz + 2) + 2LL * g.nx * g.ny;
+    k_halo<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(g, f);
+    WPF_CUDA(cudaGetLastError());
+    return WPF_OK;
+}
+
+int phys_evolve(wpf_handle* h, bool phase, double dtime) {
+    int rc = ensure_per_routine_arrays(h);
+    if (rc) return rc;
+    const Grid& g = h->g;
+    double* f = phase ? h->phase : h->concent;
+    const double* d = phase ? h->dphasedt : h->dconcentdt;
+    k_evolve<<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(g, f, d, dtime);
+    if (phase) h->kf_valid = false;
+    WPF_CUDA(cudaGetLastError());
+    return phys_halo(h, f);
+}
+
+int phys_fused_update(wpf_handle* h, double dtime, double* taumin, int32_t* overshoot,
+                      double* umax) {
+    const Grid& g = h->g;
+    int rc = upload_step_slots(h);
+    if (rc) return rc;
+    k_fused_update<<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
+        g, h->phys, h->phase, h->concent, h->pressure, h->T[0], h->T[1], h->T[2], h->flags,
+        h->phase_n, h->concent_n, dtime, h->dsc);
+    WPF_CUDA(cudaGetLastError());
+    double* t = h->phase; h->phase = h->phase_n; h->phase_n = t;
+    t = h->concent; h->concent = h->concent_n; h->concent_n = t;
+    h->vel_valid = false;
+    h->kf_valid = false;
+    return read_step_slots(h, taumin, overshoot, umax);
+}
+
+int phys_set_dirichlet(wpf_handle* h) {
+    if (h->ndir > 0) {
+        k_set_dirichlet<<<(h->ndir + 255) / 256, 256, 0, h->stream>>>(h->pressure, h->dir_idx,
+                                                                       h->dir_val, h->ndir);
+        WPF_CUDA(cudaGetLastError());
+    }
+    return WPF_OK;
+}
+
+int phys_reduce(wpf_handle* h, wpf_diag* d) {
+    const Grid& g = h->g;
+    const int nparts = g.nz + 2;
+    if (h->npartials < nparts) {
+        if (h->partials) cudaFree(h->partials);
+        h->partials = nullptr;
+        int rc = dev_alloc(h, (void**)&h->partials, sizeof(DiagPart) * nparts + 64);
+        if (rc) return rc;
+        h->npartials = nparts;
+    }
+    DiagPart* parts = reinterpret_cast<DiagPart*>(h->partials);
+    k_diag_partial<<<nparts, dim3(32, 8), 0, h->stream>>>(g, h->phys, h->prm.ix_ref, h->prm.iy_ref,
+                                                          h->prm.iz_ref, h->phase, h->concent,
+                                                          h->pressure, h->T[0], parts);
+    k_diag_final<<<1, 32, 0, h->stream>>>(parts, nparts, h->dsc + S_SUM0);
+    WPF_CUDA(cudaGetLastError());
+    WPF_CUDA(cudaMemcpyAsync(h->hsc + S_SUM0, h->dsc + S_SUM0, 8 * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    double pref = 0.0;
+    const wpf_params& p = h->prm;
+    if (p.ix_ref >= 1 && p.ix_ref <= g.nx && p.iy_ref >= 1 && p.iy_ref <= g.ny && p.iz_ref >= 1 &&
+        p.iz_ref <= g.nz) {
+        WPF_CUDA(cudaMemcpyAsync(&pref, h->pressure + g.at(p.ix_ref, p.iy_ref, p.iz_ref),
+                                 sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    const double* o = h->hsc + S_SUM0;
+    const double dx = h->phys.dx;
+    d->pv = dx * dx * dx * p.porosity * 0.5 * o[0];
+    d->vcal = dx * dx * dx * (1.0 - p.porosity) * 0.5 * o[1];
+    d->inlet_flux = o[2];
+    d->rwhmax = sqrt(o[3]);
+    d->phase_max = o[4]; d->phase_min = o[5];
+    d->concent_max = o[6]; d->concent_min = o[7];
+    d->pressure_ref = pref;
+    return WPF_OK;
+}
+
+}  // namespace wpf

@@ -1,0 +1,180 @@
+"""The CPU oracle against independent pins: a scipy direct solve of the
+system assembled exactly as the reference assembles it, analytic
+known-answer cases, and the committed golden vectors."""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+from conftest import rel_l2
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _case(n=(12, 10, 8), **kw):
+    from mizuho_edit_gb300.cases import make_case
+    return make_case(n, **kw)
+
+
+def _sim(oracle_mod, case):
+    return oracle_mod.OracleSim(case.params, case.permeab_rock, case.phase, case.concent)
+
+
+def test_assembly_matches_reference_structure(oracle_mod):
+    case = _case(seed=1)
+    s = _sim(oracle_mod, case)
+    s.calcPermeability()
+    irn, jcn, val, b = s.assemble()
+    p = case.params
+    N = p.nx * p.ny * p.nz
+    A = sp.csr_matrix((val, (irn, jcn)), shape=(N, N))
+    # entries are unique (no duplicates were summed)
+    assert A.nnz == len(val)
+    # symmetric: the Dirichlet elimination keeps A symmetric (:827-936, MAT_SYMMETRIC :945)
+    assert abs(A - A.T).max() == 0.0
+    # Dirichlet rows are identity rows with b = well pressure
+    dirs = [(w.ix - 1) + (w.iy - 1) * p.nx + (w.iz - 1) * p.nx * p.ny for w in p.wells]
+    for r in dirs[:20]:
+        row = A.getrow(r)
+        assert row.nnz == 1 and row[0, r] == 1.0
+    assert b[dirs[0]] == 1.0
+    # free rows: negative diagonal equal to minus the sum of the face transmissibilities
+    d = A.diagonal()
+    free = np.setdiff1d(np.arange(N), dirs)
+    assert np.all(d[free] < 0)
+
+
+@pytest.mark.parametrize("seed,lv", [(1, 1.0), (2, 2.5)])
+def test_solvers_match_direct(oracle_mod, seed, lv):
+    case = _case((14, 10, 9), seed=seed, log_var=lv, corr_len=3.0)
+    s = _sim(oracle_mod, case)
+    s.calcPermeability()
+    irn, jcn, val, b = s.assemble()
+    p = case.params
+    N = p.nx * p.ny * p.nz
+    A = sp.csc_matrix((val, (irn, jcn)), shape=(N, N))
+    x = spl.spsolve(A, b)
+    s2 = _sim(oracle_mod, case)
+    s2.calcPermeability()
+    info = s.solvePressure(oracle_mod.SOLVE_CG, 1e-14)
+    assert info.converged
+    pcg = s.pressure[1:-1, 1:-1, 1:-1].ravel(order="F")
+    assert rel_l2(pcg, x) < 1e-12
+    info2 = s2.solvePressure(oracle_mod.SOLVE_BCGS_SOR, 1e-10, 1000, 1)
+    assert info2.converged and info2.iterations < 1000
+    pb = s2.pressure[1:-1, 1:-1, 1:-1].ravel(order="F")
+    assert rel_l2(pb, x) < 1e-7
+    # block-local SOR (the reference under mpirun -n 4) converges to the same solution
+    s3 = _sim(oracle_mod, case)
+    s3.calcPermeability()
+    info3 = s3.solvePressure(oracle_mod.SOLVE_BCGS_SOR, 1e-10, 1000, 4)
+    assert info3.converged
+    assert rel_l2(s3.pressure[1:-1, 1:-1, 1:-1].ravel(order="F"), x) < 1e-7
+
+
+def test_homogeneous_linear_pressure(oracle_mod):
+    """Uniform K with Dirichlet planes: p is linear in x, u_x uniform."""
+    case = _case((10, 6, 5), log_var=0.0, kwh=1.0)
+    s = _sim(oracle_mod, case)
+    s.calcPermeability()
+    s.solvePressure(oracle_mod.SOLVE_CG, 1e-14)
+    p = case.params
+    x = np.arange(1, p.nx + 1)
+    expect = 1.0 - (x - 1) / (p.nx - 1) * (1.0 - 1e-300)
+    got = s.pressure[1:-1, 1:-1, 1:-1]
+    assert np.max(np.abs(got - expect[:, None, None])) < 1e-12
+    s.calcVelocity()
+    ux = s.velocity[0, 1:p.nx, 1:-1, 1:-1]
+    assert np.max(np.abs(ux - 1.0 / (p.nx - 1))) < 1e-12
+    # outer faces carry no flow (halo copy of the pressure)
+    assert np.all(s.velocity[0, 0, 1:-1, 1:-1] == 0.0)
+
+
+def test_heat_equation_concentration(oracle_mod):
+    """u = 0 and phase = -1 everywhere: dc/dt is the 7-point heat operator."""
+    from mizuho_edit_gb300.config import Well
+    case = _case((9, 8, 7), log_var=0.0)
+    p = case.params
+    p.wells = [Well(1, 1, 1, pressure=1.0, phase=-1.0, concent=0.0)]
+    rng = np.random.default_rng(0)
+    case.phase = -np.ones((p.nx, p.ny, p.nz))
+    case.concent = rng.random((p.nx, p.ny, p.nz))
+    case.concent[0, 0, 0] = 0.0
+    s = _sim(oracle_mod, case)
+    s.calcPermeability()
+    s.solvePressure(oracle_mod.SOLVE_CG, 1e-14)
+    assert np.max(np.abs(s.pressure[1:-1, 1:-1, 1:-1] - 1.0)) < 1e-13
+    s.calcVelocity()
+    assert np.max(np.abs(s.velocity)) < 1e-12
+    s.calcPhaseDeriv()
+    assert np.all(s.dphasedt == 0.0)
+    s.calcConcentDeriv()
+    c = s.concent
+    lap = (c[2:, 1:-1, 1:-1] + c[:-2, 1:-1, 1:-1] + c[1:-1, 2:, 1:-1] + c[1:-1, :-2, 1:-1]
+           + c[1:-1, 1:-1, 2:] + c[1:-1, 1:-1, :-2] - 6 * c[1:-1, 1:-1, 1:-1]) / p.dx ** 2
+    expect = p.diffusion * lap
+    expect[0, 0, 0] = 0.0     # well cell
+    assert np.max(np.abs(s.dconcentdt[1:-1, 1:-1, 1:-1] - expect)) < 1e-11
+
+
+def test_update_halo_clamps_corners(oracle_mod):
+    case = _case((4, 3, 2))
+    s = _sim(oracle_mod, case)
+    f = np.zeros((6, 5, 4), order="F")
+    f[1:-1, 1:-1, 1:-1] = np.arange(24).reshape((4, 3, 2), order="F")
+    s.updateHalo(f)
+    ii = np.clip(np.arange(6), 1, 4)
+    jj = np.clip(np.arange(5), 1, 3)
+    kk = np.clip(np.arange(4), 1, 2)
+    assert np.array_equal(f, f[np.ix_(ii, jj, kk)])
+
+
+def test_dt_law(oracle_mod):
+    case = _case()
+    s = _sim(oracle_mod, case)
+    p = case.params
+    s.taumin = 3.0
+    s.dtime = 0.123
+    assert s.next_dtime(1) == 0.123 and s.next_dtime(2) == 0.123
+    e2 = p.epsilon ** 2
+    assert s.next_dtime(3) == p.tfac * 0.5 * p.dx ** 2 / e2 * min(e2 / p.diffusion, 3.0)
+
+
+def test_trig_identities_used_by_the_kernel():
+    """The sm_103a kernel replaces atan/acos/cos/sin (wPFAW3D.f90:1289-1306) by
+    exact identities; check them against libm on random gradients."""
+    rng = np.random.default_rng(3)
+    gx, gy, gz = rng.standard_normal((3, 100000)) * np.array([[1], [1], [1e-3]])
+    gz[:100] = 0.0
+    gx[100:200] = 0.0
+    a = gx + 1e-20
+    dpf = np.sqrt(gx * gx + gy * gy + gz * gz)
+    th = np.arctan(gy / a)
+    ph = np.arccos(gz / (dpf + 1e-20))
+    c2 = a * a / (a * a + gy * gy)
+    s2 = gy * gy / (a * a + gy * gy)
+    u = gz / (dpf + 1e-20)
+    assert np.max(np.abs(c2 - np.cos(th) ** 2)) < 1e-13
+    assert np.max(np.abs(s2 - np.sin(th) ** 2)) < 1e-13
+    c = np.abs(a) / np.sqrt(a * a + gy * gy)
+    s = np.sign(a) * gy / np.sqrt(a * a + gy * gy)
+    assert np.max(np.abs(c - np.cos(th))) < 1e-13
+    assert np.max(np.abs(s - np.sin(th))) < 1e-13
+    assert np.max(np.abs(8 * u * u * (u * u - 1) + 1 - np.cos(4 * ph))) < 1e-12
+    assert np.max(np.abs(4 * u * np.sqrt(1 - u * u) * (2 * u * u - 1) - np.sin(4 * ph))) < 1e-12
+
+
+def test_golden_vectors(oracle_mod):
+    """Oracle outputs pinned by the committed fixture (tests/golden/make_golden.py)."""
+    path = os.path.join(GOLDEN, "oracle_12x10x8_s1.npz")
+    g = np.load(path)
+    case = _case((12, 10, 8), seed=1)
+    assert np.array_equal(case.permeab_rock, g["permeab_rock"])
+    s = _sim(oracle_mod, case)
+    for _ in range(int(g["steps"])):
+        s.step(oracle_mod.SOLVE_CG, 1e-14)
+    for k in ("pressure", "phase", "concent"):
+        assert rel_l2(getattr(s, k), g[k]) < 1e-12, k
+    assert s.dtime == pytest.approx(float(g["dtime"]), rel=1e-13)
