@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""Time-steps/s of the wPFAW3D time step on GB300.
+
+Workload: one 256^3 synthetic wormholing domain (K = exp(sigma g), log-K
+variance 2, correlation length 8 cells, seeded), Darcy solve to a 1e-8
+relative residual with the FP32 MG-PCG inside FP64 iterative refinement,
+then the fused phase / concentration update.  A "step" is one pass of the
+main-loop body (wPFAW3D.f90:2226-2280).  Inputs (all FP64 fields, ~2 GB)
+are far larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank advances its own replica (different seed);
+the path has no exchange step on one domain, so there is no collective in
+the timed region -- only the barrier and the max-over-ranks timing.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "time-steps/s at 256^3, 1e-8 Darcy residual (FP32-refined MG-PCG)"
+KC_NAMES = ["permeability", "resid64", "coefficients", "smooth_l0", "mg_other", "apply",
+            "pcg_vec", "fused_update", "other"]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="cells per axis")
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--log-var", type=float, default=2.0)
+    ap.add_argument("--corr", type=float, default=8.0)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--verbose", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return d["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def make_workload(args, rank):
+    from mizuho_edit_gb300.cases import make_case
+    n = args.n
+    return make_case((n, n, n), log_var=args.log_var, corr_len=args.corr, seed=args.seed + rank)
+
+
+def config_of(args, world):
+    n = args.n
+    return {"workload": f"wPFAW3D step, {n}^3 cells, synthetic GRF log-K var {args.log_var} "
+                        f"corr {args.corr}, Pe 100, Da 10, Dirichlet p 1->0",
+            "grid": [n, n, n], "solver": "fp32-mg-pcg-in-fp64-refinement" if args.solver == "mixed"
+            else "fp64-mg-pcg", "darcy_rtol": args.rtol, "dtype_state": "f64",
+            "l2_policy": "inputs larger than L2 (~2 GB of fields per step)",
+            "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
+
+
+def cpu_sample(sim, args):
+    """One reference time step (BiCGStab + SOR(10, 1.7), rtol 1e-10, the
+    reference's PETSc settings) on the host cores from the GPU run's state."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    p = sim.params
+    f = sim.download("phase", "concent", "pressure")
+    ref = O.OracleSim(p, sim._kr_cache, f["phase"][1:-1, 1:-1, 1:-1],
+                      f["concent"][1:-1, 1:-1, 1:-1])
+    ref.pressure[...] = f["pressure"]
+    ref.itime, ref.dtime, ref.taumin = sim.itime, sim.dtime, sim.taumin
+    t0 = time.perf_counter()
+    info = ref.step(O.SOLVE_BCGS_SOR, 1e-10, 1000, threads)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "time-steps/s", "cores": threads, "kind": "port",
+            "sample": f"1 reference time step at {p.nx}^3 from the benchmark's warm state "
+                      f"(BiCGStab+SOR(10,1.7) rtol 1e-10, {info.iterations} its, "
+                      f"{threads} OpenMP threads as {threads} SOR blocks), {dt:.1f} s"}
+
+
+def run_ours(args):
+    import torch
+    from mizuho_edit_gb300 import capi
+    from mizuho_edit_gb300.sim import Simulation
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    case = make_workload(args, rank)
+    sim = Simulation(case.params, case.permeab_rock, case.phase, case.concent,
+                     solver=args.solver, rtol=args.rtol)
+    L = sim.L
+    for _ in range(args.warmup):
+        sim.step()
+    sp = C.c_void_p()
+    capi.check(L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
+    stream = torch.cuda.ExternalStream(sp.value)
+    KC_SMOOTH0 = 3
+    capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    n0 = C.c_int64()
+    L.wpf_launch_count(sim.h, C.byref(n0))
+    e0.record(stream)
+    stats = [sim.step() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    n1 = C.c_int64()
+    L.wpf_launch_count(sim.h, C.byref(n1))
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    kms = (C.c_double * 9)()
+    kcnt = (C.c_int64 * 9)()
+    L.wpf_kernel_times(sim.h, kms, kcnt, 9)
+    L.wpf_set_kernel_timing(sim.h, 0)
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    n = args.n
+    ncell = n ** 3
+    value = world * args.steps / (ms_max / 1000.0)
+
+    # roofline of the finest-level red-black Gauss-Seidel smoother (the
+    # largest share of the step in the launch list): algorithmic bytes per
+    # half-sweep = couplings cx,cy,cz of every cell (12 B) + x of the other
+    # colour (2 B) + b, 1/diag and the new x of this colour (6 B) = 20 B/cell;
+    # the zero-guess first sweep reads b, 1/diag and writes x: 12 B/cell.
+    nu = 2
+    cnt = int(kcnt[KC_SMOOTH0])
+    n_first = cnt // (4 * nu)
+    n_rb = cnt - n_first
+    smooth_bytes = (n_first * 12.0 + n_rb * 20.0) * ncell
+    smooth_ms = float(kms[KC_SMOOTH0])
+    peak, peak_kind = measured_peaks()
+    achieved = smooth_bytes / (smooth_ms / 1000.0) / 1e9 if smooth_ms > 0 else None
+    roof = {"kernel": "k_rbgs<float> (finest level)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "peak_source": peak_kind, "bytes_per_cell_per_halfsweep": 20,
+            "launches": cnt, "avg_launch_us": smooth_ms * 1000.0 / max(cnt, 1)}
+
+    upd_ms = statistics.mean(s.update_ms for s in stats)
+    upd_bytes = 65.0 * ncell
+    out = {
+        "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian random field permeability; no data set)",
+        "config": config_of(args, world),
+        "cell_updates_per_s": value * ncell,
+        "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
+        "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
+        "outer_passes_per_step": statistics.mean(s.outer_iterations for s in stats),
+        "relres_max": max(s.relres for s in stats),
+        "fused_update_ms": upd_ms,
+        "fused_update_gbs": upd_bytes / (upd_ms / 1000.0) / 1e9 if upd_ms > 0 else None,
+        "gpu_launches": int(n1.value - n0.value),
+        "roofline": roof,
+        "clocks": clk,
+        "kernel_class_ms": {KC_NAMES[3]: smooth_ms},
+    }
+    if not args.no_e2e:
+        out["e2e"] = e2e_pass(args, sim, stream, world)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_sample(sim, args)
+        except Exception as e:  # the baseline must not sink the GPU line
+            out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def e2e_pass(args, sim, stream, world):
+    """Same metric through the C ABI with host-owned fields: every step uploads
+    permeab_rock, phase, concent, pressure from pinned host buffers, runs
+    wpf_step and downloads phase, concent, pressure (the reference keeps its
+    module arrays on the host)."""
+    import torch
+    from mizuho_edit_gb300 import capi
+    L = sim.L
+    sh = sim.halo_shape
+    G = sh[0] * sh[1] * sh[2]
+    bufs = {}
+    for name in ("permeab_rock", "phase", "concent", "pressure"):
+        ptr = C.c_void_p()
+        capi.check(L.wpf_host_alloc(G * 8, C.byref(ptr)), "wpf_host_alloc")
+        arr = np.ctypeslib.as_array((C.c_double * G).from_address(ptr.value))
+        bufs[name] = (ptr, arr.reshape(sh, order="F"))
+    f = sim.download("phase", "concent", "pressure")
+    for k in ("phase", "concent", "pressure"):
+        bufs[k][1][...] = f[k]
+    kr = np.zeros(sh, order="F")
+    kr[1:-1, 1:-1, 1:-1] = sim._kr_cache
+    bufs["permeab_rock"][1][...] = kr
+    dp = {k: v[1].ctypes.data_as(capi.DP) for k, v in bufs.items()}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st = capi.StepStats()
+    for _ in range(args.steps):
+        capi.check(L.wpf_upload(sim.h, dp["permeab_rock"], dp["phase"], dp["concent"],
+                                dp["pressure"]), "wpf_upload")
+        sim.itime += 1
+        dt = C.c_double(sim.dtime)
+        capi.check(L.wpf_step(sim.h, sim.itime, C.byref(dt), C.byref(st)), "wpf_step")
+        sim.dtime = dt.value
+        capi.check(L.wpf_download(sim.h, dp["phase"], dp["concent"], dp["pressure"], None, None,
+                                  None, None), "wpf_download")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    for ptr, _ in bufs.values():
+        L.wpf_host_free(ptr)
+    return {"value": world * args.steps / (ms / 1000.0), "unit": "time-steps/s",
+            "h2d_bytes_per_step": 4 * G * 8, "d2h_bytes_per_step": 3 * G * 8,
+            "path": "wpf_upload + wpf_step + wpf_download per step, pinned host buffers"}
+
+
+def run_reference(args):
+    """The reference's own CPU algorithm for this path: the reference
+    (Fortran + Intel MPI + PETSc 3.22) does not build here, so its C
+    restatement (oracle/) runs in reference-mirroring mode -- BiCGStab +
+    SOR(10, 1.7) at rtol 1e-10, warm-started, OpenMP threads as SOR blocks."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    case = make_workload(args, 0)
+    s = O.OracleSim(case.params, case.permeab_rock, case.phase, case.concent)
+    budget_w, budget_t = 150.0, 120.0
+    t0 = time.perf_counter()
+    wdone = 0
+    for _ in range(max(args.warmup, 1)):
+        s.step(O.SOLVE_BCGS_SOR, 1e-10, 1000, threads)
+        wdone += 1
+        if time.perf_counter() - t0 > budget_w:
+            break
+    times = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        s.step(O.SOLVE_BCGS_SOR, 1e-10, 1000, threads)
+        times.append(time.perf_counter() - t1)
+        if sum(times) > budget_t:
+            break
+    tot = sum(times)
+    v = len(times) / tot
+    n = args.n
+    sample = (f"{len(times)} of {args.steps} requested reference time steps at {n}^3 after "
+              f"{wdone} warm-up steps (BiCGStab+SOR(10,1.7), rtol 1e-10, {threads} OpenMP "
+              f"threads as SOR blocks), {tot:.1f} s")
+    out = {"metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": world,
+           "steps": len(times), "warmup": wdone, "ms_per_step": 1000.0 * tot / len(times),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded Gaussian random field permeability; no data set)",
+           "config": config_of(args, world), "impl": "reference",
+           "cell_updates_per_s": v * n ** 3,
+           "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

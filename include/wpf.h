@@ -91,7 +91,9 @@ typedef struct wpf_step_stats {
     double dtime;              /* dt used by this step                                  */
     double max_courant;        /* max |u| * dt / dx over faces (advection CFL)          */
     double solve_ms;           /* device time of the Darcy solve                       */
-    double update_ms;          /* device time of the rest of the step                  */
+    double update_ms;          /* device time of the fused update kernel               */
+    int32_t kernel_launches;   /* kernels this call launched                           */
+    int32_t pad;
 } wpf_step_stats;
 
 /* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */
@@ -156,6 +158,21 @@ int wpf_reduce(wpf_handle* h, wpf_diag* d);
 
 /* Last taumin on the device (the lagged input of the dt law).               */
 int wpf_get_taumin(const wpf_handle* h, double* taumin);
+
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own
+ * work or timing events with the library's; and the number of kernels the
+ * handle has launched so far.                                                */
+int wpf_get_stream(const wpf_handle* h, void** stream);
+int wpf_launch_count(const wpf_handle* h, int64_t* n);
+
+/* Per-kernel-class device timers (CUDA events around each launch of the
+ * classes in `mask`; bit c = class c): 0 permeability, 1 FP64 residual,
+ * 2 solver coefficients, 3 finest-level smoother, 4 other multigrid kernels,
+ * 5 PCG operator apply, 6 PCG vector kernels, 7 fused update, 8 other.
+ * Setting the mask resets the totals; wpf_kernel_times returns the summed
+ * milliseconds and launch counts of the first n classes.                  */
+int wpf_set_kernel_timing(wpf_handle* h, uint32_t mask);
+int wpf_kernel_times(wpf_handle* h, double* ms, int64_t* counts, int32_t n);
 
 /* Page-locked host buffers for callers that stream fields every step (the
  * copies in wpf_upload / wpf_download then run at full link bandwidth).     */

@@ -54,7 +54,8 @@ class StepStats(C.Structure):
     _fields_ = [("outer_iterations", C.c_int32), ("inner_iterations", C.c_int32),
                 ("converged", C.c_int32), ("overshoot_cells", C.c_int32), ("relres", C.c_double),
                 ("taumin", C.c_double), ("dtime", C.c_double), ("max_courant", C.c_double),
-                ("solve_ms", C.c_double), ("update_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("update_ms", C.c_double),
+                ("kernel_launches", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -95,6 +96,10 @@ SIGNATURES = {
     "wpf_run": (C.c_int, [H, C.c_int32, C.c_int32, DP, C.POINTER(StepStats)]),
     "wpf_reduce": (C.c_int, [H, C.POINTER(Diag)]),
     "wpf_get_taumin": (C.c_int, [H, DP]),
+    "wpf_get_stream": (C.c_int, [H, C.POINTER(C.c_void_p)]),
+    "wpf_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
+    "wpf_set_kernel_timing": (C.c_int, [H, C.c_uint32]),
+    "wpf_kernel_times": (C.c_int, [H, DP, C.POINTER(C.c_int64), C.c_int32]),
     "wpf_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
     "wpf_host_free": (C.c_int, [C.c_void_p]),
 }

@@ -27,6 +27,35 @@ int dev_alloc(wpf_handle* h, void** p, size_t bytes) {
     return WPF_OK;
 }
 
+int timer_start(wpf_handle* h, int c) {
+    if (!(h->timing_mask & (1u << c))) return -1;
+    if (h->npend >= 256) timer_flush(h);
+    if (h->npend >= 256) return -1;
+    const int slot = h->npend++;
+    h->pend_cls[slot] = c;
+    cudaEventRecord(h->pend_ev[2 * slot], h->stream);
+    return slot;
+}
+
+void timer_stop(wpf_handle* h, int slot) {
+    if (slot >= 0) cudaEventRecord(h->pend_ev[2 * slot + 1], h->stream);
+}
+
+void timer_flush(wpf_handle* h) {
+    if (!h->npend) return;
+    cudaEventSynchronize(h->pend_ev[2 * h->npend - 1]);
+    for (int s = 0; s < h->npend; ++s) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->pend_ev[2 * s], h->pend_ev[2 * s + 1]) == cudaSuccess) {
+            h->kt_ms[h->pend_cls[s]] += ms;
+            h->kt_count[h->pend_cls[s]] += 1;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    h->npend = 0;
+}
+
 int ensure_per_routine_arrays(wpf_handle* h) {
     if (h->K0) return WPF_OK;
     const size_t b = sizeof(double) * h->g.total;
@@ -77,6 +106,8 @@ static void free_all(wpf_handle* h) {
     if (h->hsc) cudaFreeHost(h->hsc);
     for (int e = 0; e < 4; ++e)
         if (h->ev[e]) cudaEventDestroy(h->ev[e]);
+    for (int e = 0; e < 512; ++e)
+        if (h->pend_ev[e]) cudaEventDestroy(h->pend_ev[e]);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -381,16 +412,15 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     wpf_step_stats tmp;
     memset(&tmp, 0, sizeof(tmp));
     wpf_step_stats* s = st ? st : &tmp;
+    const long long l0 = h->nlaunch;
     int rc = phys_permeability(h, false);
     if (rc) return rc;
     const int srs = solve_pressure(h, s);
     if (srs && srs != WPF_ERR_NOT_CONVERGED) return srs;
-    WPF_CUDA(cudaEventRecord(h->ev[2], h->stream));
     double taumin = 0, umax = 0;
     int32_t over = 0;
-    rc = phys_fused_update(h, dt, &taumin, &over, &umax);
+    rc = phys_fused_update(h, dt, &taumin, &over, &umax);   // records ev[2]/ev[3] around the kernel
     if (rc) return rc;
-    WPF_CUDA(cudaEventRecord(h->ev[3], h->stream));
     WPF_CUDA(cudaEventSynchronize(h->ev[3]));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
@@ -399,6 +429,7 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     s->overshoot_cells = over;
     s->dtime = dt;
     s->max_courant = umax * dt / p.dx;
+    s->kernel_launches = (int32_t)(h->nlaunch - l0);
     *dtime_inout = dt;
     return srs;
 }
@@ -412,6 +443,38 @@ int wpf_run(wpf_handle* h, int32_t itime0, int32_t nsteps, double* dtime_inout,
         if (rc && rc != WPF_ERR_NOT_CONVERGED) return rc;
     }
     return rc;
+}
+
+int wpf_set_kernel_timing(wpf_handle* h, uint32_t mask) {
+    if (!h) return WPF_ERR_ARG;
+    if (mask && !h->pend_ev[0]) {
+        for (int e = 0; e < 512; ++e)
+            if (cudaEventCreate(&h->pend_ev[e]) != cudaSuccess) return WPF_ERR_CUDA;
+    }
+    timer_flush(h);
+    h->timing_mask = mask & ((1u << KC_COUNT) - 1);
+    for (int c = 0; c < 16; ++c) { h->kt_ms[c] = 0.0; h->kt_count[c] = 0; }
+    return WPF_OK;
+}
+
+int wpf_kernel_times(wpf_handle* h, double* ms, int64_t* counts, int32_t n) {
+    if (!h || n < 0 || (n > 0 && (!ms || !counts))) return WPF_ERR_ARG;
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    timer_flush(h);
+    for (int c = 0; c < n && c < 16; ++c) { ms[c] = h->kt_ms[c]; counts[c] = h->kt_count[c]; }
+    return WPF_OK;
+}
+
+int wpf_get_stream(const wpf_handle* h, void** stream) {
+    if (!h || !stream) return WPF_ERR_ARG;
+    *stream = (void*)h->stream;
+    return WPF_OK;
+}
+
+int wpf_launch_count(const wpf_handle* h, int64_t* n) {
+    if (!h || !n) return WPF_ERR_ARG;
+    *n = h->nlaunch;
+    return WPF_OK;
 }
 
 int wpf_host_alloc(int64_t bytes, void** ptr) {

@@ -120,7 +120,45 @@ struct wpf_handle {
     int64_t bytes;           // device bytes allocated
     bool vel_valid;
     bool kf_valid;           // Kf/K0 hold calcPermeability of the current phase
+    long long nlaunch;       // kernels launched on this handle so far
+    // per-kernel-class event timers (enabled by wpf_set_kernel_timing)
+    unsigned timing_mask;
+    int npend;
+    int pend_cls[256];
+    cudaEvent_t pend_ev[512];
+    double kt_ms[16];
+    long long kt_count[16];
 };
+
+namespace wpf {
+// Kernel classes for the event timers (bit i of wpf_set_kernel_timing's mask).
+enum KClass {
+    KC_PERM = 0,      // calcPermeability face kernel
+    KC_RESID64,       // FP64 outer residual
+    KC_COEF,          // level-0 coefficients + coarsening
+    KC_SMOOTH0,       // red-black Gauss-Seidel on the finest level
+    KC_MGREST,        // other multigrid kernels (restrict, prolong, coarse levels)
+    KC_APPLY,         // PCG operator apply + dot
+    KC_VEC,           // PCG vector updates / dots / correction
+    KC_FUSED,         // fused velocity + phase + concentration + Euler + halo
+    KC_OTHER,         // halo, Dirichlet, reductions
+    KC_COUNT
+};
+// Record a start event for class c (if timed); returns the slot or -1.
+int timer_start(wpf_handle* h, int c);
+void timer_stop(wpf_handle* h, int slot);
+void timer_flush(wpf_handle* h);   // after a synchronisation: fold finished pairs
+}  // namespace wpf
+
+// Launch a kernel on the handle's stream: counts it and, if its class is
+// timed, brackets it with a pair of events.
+#define WPF_LAUNCH(h, cls, ...)                               \
+    do {                                                      \
+        const int ts_ = ::wpf::timer_start((h), (cls));       \
+        ++(h)->nlaunch;                                       \
+        __VA_ARGS__;                                          \
+        ::wpf::timer_stop((h), ts_);                          \
+    } while (0)
 
 namespace wpf {
 

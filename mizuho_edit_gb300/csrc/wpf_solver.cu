@@ -404,13 +404,13 @@ template <typename R>
 static int build_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
     const Grid& g = h->g;
     Level<R>& L0 = H.lv[0];
-    k_l0_coeffs<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
-        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag);
+    WPF_LAUNCH(h, KC_COEF, k_l0_coeffs<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
+        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag));
     for (int l = 0; l + 1 < H.nlev; ++l) {
         Level<R>& F = H.lv[l];
         Level<R>& C = H.lv[l + 1];
-        k_coarsen<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, h->stream>>>(
-            F.g, C.g, F.cx, F.cy, F.cz, F.diag, C.cx, C.cy, C.cz, C.diag, C.idiag, (R)COARSE_SCALE);
+        WPF_LAUNCH(h, KC_COEF, k_coarsen<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, h->stream>>>(
+            F.g, C.g, F.cx, F.cy, F.cz, F.diag, C.cx, C.cy, C.cz, C.diag, C.idiag, (R)COARSE_SCALE));
     }
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
@@ -431,31 +431,31 @@ static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu) {
         Level<R>& L = H.lv[l];
         const Grid& g = L.g;
         if (l == H.nlev - 1) {
-            k_coarse_solve<R><<<1, 256, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 16);
+            WPF_LAUNCH(h, KC_MGREST, k_coarse_solve<R><<<1, 256, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 16));
             break;
         }
         dim3 b, gr;
         rbgs_grid<R>(g, gr, b);
-        k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b);
-        k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1);
+        WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b));
+        WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
         for (int it = 1; it < nu; ++it) {
-            k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0);
-            k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1);
+            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
         }
         Level<R>& C = H.lv[l + 1];
-        k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
-            g, C.g, L.cx, L.cy, L.cz, L.diag, L.x, L.b, C.b, C.x);
+        WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
+            g, C.g, L.cx, L.cy, L.cz, L.diag, L.x, L.b, C.b, C.x));
     }
     for (int l = H.nlev - 2; l >= 0; --l) {
         Level<R>& L = H.lv[l];
         Level<R>& C = H.lv[l + 1];
         const Grid& g = L.g;
-        k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x);
+        WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x));
         dim3 b, gr;
         rbgs_grid<R>(g, gr, b);
         for (int it = 0; it < nu; ++it) {
-            k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1);
-            k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0);
+            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
         }
     }
 }
@@ -464,6 +464,7 @@ static int read_slot(wpf_handle* h, int slot, int n = 1) {
     WPF_CUDA(cudaMemcpyAsync(h->hsc + slot, h->dsc + slot, n * sizeof(double), cudaMemcpyDeviceToHost,
                              h->stream));
     WPF_CUDA(cudaStreamSynchronize(h->stream));
+    timer_flush(h);
     return WPF_OK;
 }
 
@@ -477,13 +478,13 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
     dim3 gr = cell_grid(g.nx, g.ny, g.nz), b = cell_block();
     Level<R>& L0 = H.lv[0];
     double* d = h->dsc;
-    k_zero_interior<R><<<gr, b, 0, s>>>(g, H.x);
+    WPF_LAUNCH(h, KC_VEC, k_zero_interior<R><<<gr, b, 0, s>>>(g, H.x));
     WPF_CUDA(cudaMemsetAsync(d + S_RZ0, 0, 2 * sizeof(double), s));
     WPF_CUDA(cudaMemsetAsync(d + S_RR, 0, sizeof(double), s));
-    k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.r, d + S_RR);
+    WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.r, d + S_RR));
     vcycle(h, H, nu);
-    k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0);
-    k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0, d + S_RZ0, 1);
+    WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0));
+    WPF_LAUNCH(h, KC_VEC, k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0, d + S_RZ0, 1));
     int rc = read_slot(h, S_RR);
     if (rc) return rc;
     const double r0 = sqrt(h->hsc[S_RR]);
@@ -493,8 +494,8 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
     int cur = 0;
     for (int it = 0; it < maxit; ++it) {
         WPF_CUDA(cudaMemsetAsync(d + S_PQ, 0, 2 * sizeof(double), s));   // S_PQ, S_RR
-        k_apply_dot<R><<<gr, b, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.p, H.q, d + S_PQ);
-        k_update_xr<R><<<gr, b, 0, s>>>(g, H.x, H.r, H.p, H.q, d + S_RZ0 + cur, d + S_PQ, d + S_RR);
+        WPF_LAUNCH(h, KC_APPLY, k_apply_dot<R><<<gr, b, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.p, H.q, d + S_PQ));
+        WPF_LAUNCH(h, KC_VEC, k_update_xr<R><<<gr, b, 0, s>>>(g, H.x, H.r, H.p, H.q, d + S_RZ0 + cur, d + S_PQ, d + S_RR));
         rc = read_slot(h, S_PQ, 2);
         if (rc) return rc;
         *iters = it + 1;
@@ -505,8 +506,8 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
         vcycle(h, H, nu);
         const int nxt = cur ^ 1;
         WPF_CUDA(cudaMemsetAsync(d + S_RZ0 + nxt, 0, sizeof(double), s));
-        k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0 + nxt);
-        k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0 + nxt, d + S_RZ0 + cur, 0);
+        WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0 + nxt));
+        WPF_LAUNCH(h, KC_VEC, k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0 + nxt, d + S_RZ0 + cur, 0));
         cur = nxt;
     }
     return WPF_ERR_NOT_CONVERGED;
@@ -543,8 +544,8 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     double relres = 0.0, bnorm = 0.0;
     for (int pass = 0; pass <= h->opts.max_outer; ++pass) {
         WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 2 * sizeof(double), s));
-        k_resid64<R><<<gr, b, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm,
-                                      H.r, h->dsc, pass == 0);
+        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<gr, b, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm,
+                                      H.r, h->dsc, pass == 0));
         WPF_CUDA(cudaGetLastError());
         rc = read_slot(h, S_RR64, 2);
         if (rc) return rc;
@@ -562,7 +563,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         rc = pcg<R>(h, H, tol, h->opts.max_inner, nu, &its, &ratio);
         inner_total += its;
         if (rc == WPF_ERR_NONFINITE) { status = rc; break; }
-        k_add_correction<R><<<gr, b, 0, s>>>(g, h->pressure, H.x);
+        WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<gr, b, 0, s>>>(g, h->pressure, H.x));
         WPF_CUDA(cudaGetLastError());
     }
     if (st) {

@@ -33,8 +33,10 @@ def _rough_state(case, seed=5, overshoot=0.0):
     g = grf((p.nx, p.ny, p.nz), 2.0, seed)
     ph = np.tanh(1.5 * g)
     if overshoot:
+        # overshoot on the liquid side only, where K = kwh f + Krock (1 - f)
+        # stays positive for f = (1 + phase)/2 > 1 (kwh >> Krock there)
         rng = np.random.default_rng(seed)
-        ph = ph * (1.0 + overshoot * rng.random(ph.shape))
+        ph = np.where(ph > 0, ph * (1.0 + overshoot * rng.random(ph.shape)), ph)
     ph[0] = 1.0
     ph[-1] = -1.0
     cc = np.clip(0.5 + 0.5 * grf((p.nx, p.ny, p.nz), 3.0, seed + 1), 0, 1)
