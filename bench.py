@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="time every kernel class (diagnostic run; adds event overhead)")
     return ap.parse_args()
 
 
@@ -180,7 +182,8 @@ def run_ours(args):
     capi.check(L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
     stream = torch.cuda.ExternalStream(sp.value)
     KC_SMOOTH0 = 3
-    capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
+    mask = (1 << len(KC_NAMES)) - 1 if args.breakdown else (1 << KC_SMOOTH0)
+    capi.check(L.wpf_set_kernel_timing(sim.h, mask), "timing")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         torch.distributed.barrier()
@@ -246,7 +249,11 @@ def run_ours(args):
         "gpu_launches": int(n1.value - n0.value),
         "roofline": roof,
         "clocks": clk,
-        "kernel_class_ms": {KC_NAMES[3]: smooth_ms},
+        "kernel_class_ms": ({KC_NAMES[c]: float(kms[c]) / args.steps for c in range(9)}
+                            if args.breakdown else {KC_NAMES[3]: smooth_ms / args.steps}),
+        "kernel_class_launches": ({KC_NAMES[c]: int(kcnt[c]) // args.steps for c in range(9)}
+                                  if args.breakdown else None),
+        "relres0_mean": statistics.mean(s.relres0 for s in stats),
     }
     if not args.no_e2e:
         out["e2e"] = e2e_pass(args, sim, stream, world)

@@ -94,6 +94,7 @@ typedef struct wpf_step_stats {
     double update_ms;          /* device time of the fused update kernel               */
     int32_t kernel_launches;   /* kernels this call launched                           */
     int32_t pad;
+    double relres0;            /* relative residual of the warm start                  */
 } wpf_step_stats;
 
 /* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */

@@ -55,7 +55,7 @@ class StepStats(C.Structure):
                 ("converged", C.c_int32), ("overshoot_cells", C.c_int32), ("relres", C.c_double),
                 ("taumin", C.c_double), ("dtime", C.c_double), ("max_courant", C.c_double),
                 ("solve_ms", C.c_double), ("update_ms", C.c_double),
-                ("kernel_launches", C.c_int32), ("pad", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("pad", C.c_int32), ("relres0", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

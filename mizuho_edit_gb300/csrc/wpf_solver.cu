@@ -541,7 +541,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     if (rc) return rc;
     const int nu = h->opts.smooth_sweeps > 0 ? h->opts.smooth_sweeps : 2;
     int outer = 0, inner_total = 0, status = WPF_ERR_NOT_CONVERGED;
-    double relres = 0.0, bnorm = 0.0;
+    double relres = 0.0, bnorm = 0.0, relres0 = 0.0;
     for (int pass = 0; pass <= h->opts.max_outer; ++pass) {
         WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 2 * sizeof(double), s));
         WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<gr, b, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm,
@@ -552,6 +552,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         if (pass == 0) bnorm = sqrt(h->hsc[S_BB64]);
         const double rnorm = sqrt(h->hsc[S_RR64]);
         relres = bnorm > 0.0 ? rnorm / bnorm : rnorm;
+        if (pass == 0) relres0 = relres;
         if (!(relres == relres) || isinf(relres)) { status = WPF_ERR_NONFINITE; break; }
         if (relres <= h->opts.rtol) { status = WPF_OK; break; }
         if (pass == h->opts.max_outer) break;
@@ -571,6 +572,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         st->inner_iterations = inner_total;
         st->converged = status == WPF_OK;
         st->relres = relres;
+        st->relres0 = relres0;
     }
     return status;
 }

@@ -142,14 +142,17 @@ def test_routines_one_step(oracle_mod, overshoot, ral):
         assert rel_l2(f["concent"], ref.concent) < 1e-12
 
 
-def test_fused_matches_unfused(oracle_mod):
-    case = _rough_state(_case((18, 16, 14), seed=8), overshoot=0.2)
+@pytest.mark.parametrize("overshoot,steps", [(0.0, 5), (0.3, 1)])
+def test_fused_matches_unfused(oracle_mod, overshoot, steps):
+    """The fused kernel equals the per-routine chain; with overshoot (the
+    anisotropic full path) one step from the rough state."""
+    case = _rough_state(_case((18, 16, 14), seed=8), overshoot=overshoot)
     _, Simulation = _sim_mod()
     p = case.params
     a = Simulation(p, case.permeab_rock, case.phase, case.concent, rtol=1e-13)
     b = Simulation(p, case.permeab_rock, case.phase, case.concent, rtol=1e-13)
     with a, b:
-        for _ in range(5):
+        for _ in range(steps):
             a.step()
             b.step_unfused()
         fa = a.download("phase", "concent", "pressure")
