@@ -26,6 +26,15 @@
 // down to <= 2 cells per axis, solved by Gauss-Seidel sweeps in one block.
 // Dead cells (Dirichlet, or aggregates of only Dirichlet cells) carry a zero
 // diagonal and zero couplings and never change.
+//
+// One red-black sweep is one kernel (k_sweep): each block owns a 32x8 column
+// of cells and a 32-plane chunk of z, keeps a four-plane ring of x in shared
+// memory and marches up in z, updating the first colour of plane k+1 and then
+// the second colour of plane k.  The first colour is recomputed on a one-cell
+// ring around the tile from the old values (it depends on old values only),
+// so every block produces exactly the two-kernel red-black result; the sweep
+// reads x from one buffer and writes the other, so no block can see another
+// block's new values.
 #include <math.h>
 #include <stdio.h>
 
@@ -34,6 +43,8 @@
 namespace wpf {
 
 constexpr double COARSE_SCALE = 0.5;
+constexpr int SX = 32, SY = 8, SZC = 32;   // sweep tile (x, y) and z chunk
+constexpr int FX = SX + 4, FY = SY + 4;    // shared footprint: tile + 2-cell ring
 
 // ---------------------------------------------------------------------------
 // FP64 outer residual.  r = qterm + sum_f T_f (p_nb - p_c) on free cells, 0 on
@@ -41,26 +52,22 @@ constexpr double COARSE_SCALE = 0.5;
 // b_ref the reference right-hand side (:803-825, :852-931).
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_resid64(Grid g, const double* __restrict__ pr,
-                                                 const double* __restrict__ Tx,
-                                                 const double* __restrict__ Ty,
-                                                 const double* __restrict__ Tz,
-                                                 const uint8_t* __restrict__ fl,
-                                                 const double* __restrict__ qterm,
-                                                 R* __restrict__ rout, double* dsc, int want_b) {
-    __shared__ double sm[32];
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+__global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict__ pr,
+                                                const double* __restrict__ Tx,
+                                                const double* __restrict__ Ty,
+                                                const double* __restrict__ Tz,
+                                                const uint8_t* __restrict__ fl,
+                                                const double* __restrict__ qterm,
+                                                R* __restrict__ rout, double* dsc, int want_b) {
     double rr = 0.0, bb = 0.0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+    const long long sy = g.P, sz = g.S;
+    ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
-        const long long sy = g.P, sz = g.S;
         const uint8_t f = fl[n];
         double r = 0.0;
         const double p0 = pr[n];
         if (f & F_DIR) {
-            bb = p0 * p0;
+            bb += p0 * p0;
         } else {
             const double q = qterm ? qterm[n] : 0.0;
             const double txp = Tx[n], txm = Tx[n - 1], typ = Ty[n], tym = Ty[n - sy];
@@ -77,52 +84,48 @@ __global__ void __launch_bounds__(256) k_resid64(Grid g, const double* __restric
                 if (fl[n + 1] & F_DIR) bref -= pxp * txp;
                 if (fl[n + sy] & F_DIR) bref -= pyp * typ;
                 if (fl[n + sz] & F_DIR) bref -= pzp * tzp;
-                bb = bref * bref;
+                bb += bref * bref;
             }
         }
         rout[n] = (R)r;
-        rr = r * r;
+        rr += r * r;
     }
-    rr = block_sum(rr, sm);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicAdd(dsc + S_RR64, rr);
-    if (want_b) {
-        bb = block_sum(bb, sm);
-        if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicAdd(dsc + S_BB64, bb);
-    }
+    block_add(rr, dsc + S_RR64);
+    if (want_b) block_add(bb, dsc + S_BB64);
 }
 
 // p += e on the interior (e is zero on dead cells).
 template <typename R>
-__global__ void k_add_correction(Grid g, double* __restrict__ pr, const R* __restrict__ e) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
-    pr[n] += (double)e[n];
+__global__ void __launch_bounds__(RB) k_add_correction(Grid g, double* __restrict__ pr,
+                                                       const R* __restrict__ e) {
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        pr[n] += (double)e[n];
+    }
 }
 
 // Level-0 coefficients of A' from T and the Dirichlet flags.
 template <typename R>
-__global__ void k_l0_coeffs(Grid g, const double* __restrict__ Tx, const double* __restrict__ Ty,
-                            const double* __restrict__ Tz, const uint8_t* __restrict__ fl,
-                            R* __restrict__ cx, R* __restrict__ cy, R* __restrict__ cz,
-                            R* __restrict__ diag, R* __restrict__ idiag) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
+__global__ void __launch_bounds__(RB) k_l0_coeffs(Grid g, const double* __restrict__ Tx,
+                                                  const double* __restrict__ Ty,
+                                                  const double* __restrict__ Tz,
+                                                  const uint8_t* __restrict__ fl,
+                                                  R* __restrict__ cx, R* __restrict__ cy,
+                                                  R* __restrict__ cz, R* __restrict__ diag,
+                                                  R* __restrict__ idiag) {
     const long long sy = g.P, sz = g.S;
-    const bool live = !(fl[n] & F_DIR);
-    const double tx = Tx[n], ty = Ty[n], tz = Tz[n];
-    const double d = tx + Tx[n - 1] + ty + Ty[n - sy] + tz + Tz[n - sz];
-    cx[n] = (R)((live && !(fl[n + 1] & F_DIR)) ? tx : 0.0);
-    cy[n] = (R)((live && !(fl[n + sy] & F_DIR)) ? ty : 0.0);
-    cz[n] = (R)((live && !(fl[n + sz] & F_DIR)) ? tz : 0.0);
-    const R dr = (R)(live ? d : 0.0);
-    diag[n] = dr;
-    idiag[n] = (live && dr > (R)0) ? (R)1 / dr : (R)0;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        const bool live = !(fl[n] & F_DIR);
+        const double tx = Tx[n], ty = Ty[n], tz = Tz[n];
+        const double d = tx + Tx[n - 1] + ty + Ty[n - sy] + tz + Tz[n - sz];
+        cx[n] = (R)((live && !(fl[n + 1] & F_DIR)) ? tx : 0.0);
+        cy[n] = (R)((live && !(fl[n + sy] & F_DIR)) ? ty : 0.0);
+        cz[n] = (R)((live && !(fl[n + sz] & F_DIR)) ? tz : 0.0);
+        const R dr = (R)(live ? d : 0.0);
+        diag[n] = dr;
+        idiag[n] = (live && dr > (R)0) ? (R)1 / dr : (R)0;
+    }
 }
 
 // Coarse operator of level l+1 from level l (see the file header).
@@ -172,40 +175,106 @@ __device__ __forceinline__ R offsum(const R* __restrict__ cx, const R* __restric
            cz[n] * x[n + sz] + cz[n - sz] * x[n - sz];
 }
 
-// One colour of red-black Gauss-Seidel.  Thread (t,j,k) handles the cell of
-// colour `color` ((i+j+k) & 1) at i = 1 + 2t + ((color+1+j+k) & 1).
+// ---------------------------------------------------------------------------
+// One full red-black Gauss-Seidel sweep (first colour c0, then 1-c0) from
+// xin to xout.  zero_init: xin is taken as zero (first pre-smoothing sweep).
+// xc != null: the coarse correction x_{l+1}(parent) is added to every old
+// value as it is loaded (prolongation fused into the first post sweep).
+// dot != null: accumulate b.xout (the PCG r.z, level 0 only).
+// ---------------------------------------------------------------------------
 template <typename R>
-__global__ void k_rbgs(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
-                       const R* __restrict__ cz, const R* __restrict__ idiag, R* __restrict__ x,
-                       const R* __restrict__ b, int color) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    const int i = 1 + 2 * t + ((color + 1 + j + k) & 1);
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
-    x[n] = idiag[n] * (b[n] + offsum(cx, cy, cz, x, n, g.P, g.S));
+__global__ void __launch_bounds__(SX * SY) k_sweep(Grid g, const R* __restrict__ cx,
+                                                   const R* __restrict__ cy,
+                                                   const R* __restrict__ cz,
+                                                   const R* __restrict__ idiag,
+                                                   const R* __restrict__ b,
+                                                   const R* __restrict__ xin, R* __restrict__ xout,
+                                                   int c0, int zero_init, const R* __restrict__ xc,
+                                                   Grid gc, double* dot) {
+    __shared__ R xs[4][FY][FX];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * SX + tx;
+    const int i0 = 1 + blockIdx.x * SX, j0 = 1 + blockIdx.y * SY;
+    const int k0 = 1 + blockIdx.z * SZC;
+    const int k1 = min(g.nz, k0 + SZC - 1);
+    const long long sy = g.P, sz = g.S;
+    R dacc = 0;
+
+    auto load_plane = [&](int k) {
+        R(*P)[FX] = xs[k & 3];
+        for (int q = tid; q < FX * FY; q += SX * SY) {
+            const int fj = q / FX, fi = q - fj * FX;
+            const int i = i0 - 2 + fi, j = j0 - 2 + fj;
+            R v = 0;
+            if (!zero_init && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz) {
+                v = xin[g.at(i, j, k)];
+                if (xc) v += xc[gc.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+            }
+            P[fj][fi] = v;
+        }
+    };
+    // first colour of plane k on the tile and its one-cell ring, in place
+    auto first_colour = [&](int k) {
+        if (k < 1 || k > g.nz) return;
+        R(*P)[FX] = xs[k & 3];
+        R(*Pm)[FX] = xs[(k - 1) & 3];
+        R(*Pp)[FX] = xs[(k + 1) & 3];
+        for (int q = tid; q < (FX - 2) * (FY - 2); q += SX * SY) {
+            const int fj = 1 + q / (FX - 2), fi = 1 + q % (FX - 2);
+            const int i = i0 - 2 + fi, j = j0 - 2 + fj;
+            if (i < 1 || i > g.nx || j < 1 || j > g.ny || ((i + j + k) & 1) != c0) continue;
+            const long long n = g.at(i, j, k);
+            const R s = b[n] + cx[n] * P[fj][fi + 1] + cx[n - 1] * P[fj][fi - 1] +
+                        cy[n] * P[fj + 1][fi] + cy[n - sy] * P[fj - 1][fi] + cz[n] * Pp[fj][fi] +
+                        cz[n - sz] * Pm[fj][fi];
+            P[fj][fi] = idiag[n] * s;
+        }
+    };
+    // second colour of plane k on the tile; writes both colours of the tile
+    auto second_colour = [&](int k) {
+        R(*P)[FX] = xs[k & 3];
+        R(*Pm)[FX] = xs[(k - 1) & 3];
+        R(*Pp)[FX] = xs[(k + 1) & 3];
+        const int i = i0 + tx, j = j0 + ty, fi = tx + 2, fj = ty + 2;
+        if (i <= g.nx && j <= g.ny) {
+            const long long n = g.at(i, j, k);
+            R v = P[fj][fi];
+            if (((i + j + k) & 1) != c0) {
+                const R s = b[n] + cx[n] * P[fj][fi + 1] + cx[n - 1] * P[fj][fi - 1] +
+                            cy[n] * P[fj + 1][fi] + cy[n - sy] * P[fj - 1][fi] + cz[n] * Pp[fj][fi] +
+                            cz[n - sz] * Pm[fj][fi];
+                v = idiag[n] * s;
+            }
+            xout[n] = v;
+            if (dot) dacc += b[n] * v;
+        }
+    };
+
+    load_plane(k0 - 2);
+    load_plane(k0 - 1);
+    load_plane(k0);
+    __syncthreads();
+    first_colour(k0 - 1);
+    __syncthreads();
+    load_plane(k0 + 1);
+    __syncthreads();
+    first_colour(k0);
+    for (int k = k0; k <= k1; ++k) {
+        __syncthreads();           // slot (k+2)&3 held plane k-2, read by the previous step
+        load_plane(k + 2);
+        __syncthreads();
+        first_colour(k + 1);
+        __syncthreads();
+        second_colour(k);
+    }
+    if (dot) block_add(dacc, dot);
 }
 
-// First red sweep from a zero initial guess: red cells get idiag*b, black 0.
-template <typename R>
-__global__ void k_rbgs_first(Grid g, const R* __restrict__ idiag, R* __restrict__ x,
-                             const R* __restrict__ b) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
-    x[n] = ((i + j + k) & 1) ? (R)0 : idiag[n] * b[n];
-}
-
-// Residual of level l restricted (summed over the aggregate) into b of level
-// l+1; x of level l+1 is zeroed.
+// Residual of level l restricted (summed over the aggregate) into b of level l+1.
 template <typename R>
 __global__ void k_resid_restrict(Grid f, Grid c, const R* __restrict__ cx, const R* __restrict__ cy,
                                  const R* __restrict__ cz, const R* __restrict__ diag,
                                  const R* __restrict__ x, const R* __restrict__ b,
-                                 R* __restrict__ bc, R* __restrict__ xc) {
+                                 R* __restrict__ bc) {
     const int I = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int J = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int K = 1 + blockIdx.z * blockDim.z + threadIdx.z;
@@ -225,21 +294,7 @@ __global__ void k_resid_restrict(Grid f, Grid c, const R* __restrict__ cx, const
             }
         }
     }
-    const long long m = c.at(I, J, K);
-    bc[m] = s;
-    xc[m] = 0;
-}
-
-// x_l += x_{l+1}(parent) on live cells.
-template <typename R>
-__global__ void k_prolong(Grid f, Grid c, const R* __restrict__ idiag, R* __restrict__ x,
-                          const R* __restrict__ xc) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > f.nx || j > f.ny || k > f.nz) return;
-    const long long n = f.at(i, j, k);
-    if (idiag[n] != (R)0) x[n] += xc[c.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+    bc[c.at(I, J, K)] = s;
 }
 
 // Coarsest level: Gauss-Seidel sweeps in one block from x = 0.
@@ -265,92 +320,71 @@ __global__ void k_coarse_solve(Grid g, const R* __restrict__ cx, const R* __rest
         }
 }
 
-// ---- PCG vector kernels ----------------------------------------------------
-// q = A' p, accumulate p.q.
+// ---- PCG vector kernels (persistent row loops, one atomic per block) -------
+// p_new = z + beta p_old (beta = rz_new/rz_old, 0 when first) formed on the
+// fly for the cell and its six neighbours; q = A' p_new; accumulates p_new.q.
 template <typename R>
-__global__ void __launch_bounds__(256) k_apply_dot(Grid g, const R* __restrict__ cx,
-                                                   const R* __restrict__ cy,
-                                                   const R* __restrict__ cz,
-                                                   const R* __restrict__ diag,
-                                                   const R* __restrict__ p, R* __restrict__ q,
-                                                   double* acc) {
-    __shared__ R sm[32];
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+__global__ void __launch_bounds__(RB) k_apply_p(Grid g, const R* __restrict__ cx,
+                                                const R* __restrict__ cy,
+                                                const R* __restrict__ cz,
+                                                const R* __restrict__ diag,
+                                                const R* __restrict__ z,
+                                                const R* __restrict__ pold,
+                                                R* __restrict__ pnew, R* __restrict__ q,
+                                                const double* __restrict__ rz_new,
+                                                const double* __restrict__ rz_old, int first,
+                                                double* acc) {
+    __shared__ R sbeta;
+    if (threadIdx.x == 0) sbeta = first ? (R)0 : (R)(*rz_new / *rz_old);
+    __syncthreads();
+    const R beta = sbeta;
+    const long long sy = g.P, sz = g.S;
     R d = 0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+    ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
-        const R pn = p[n];
-        const R v = diag[n] * pn - offsum(cx, cy, cz, p, n, g.P, g.S);
+        auto P = [&](long long m) { return first ? z[m] : z[m] + beta * pold[m]; };
+        const R pc = P(n);
+        const R v = diag[n] * pc - (cx[n] * P(n + 1) + cx[n - 1] * P(n - 1) + cy[n] * P(n + sy) +
+                                    cy[n - sy] * P(n - sy) + cz[n] * P(n + sz) + cz[n - sz] * P(n - sz));
+        pnew[n] = pc;
         q[n] = v;
-        d = pn * v;
+        d += pc * v;
     }
-    d = block_sum(d, sm);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicAdd(acc, (double)d);
+    block_add(d, acc);
 }
 
-// alpha = rz/pq; x += alpha p; r -= alpha q; accumulate r.r
+// alpha = rz/pq; x += alpha p (x = alpha p when first); r -= alpha q; accumulate r.r
 template <typename R>
-__global__ void __launch_bounds__(256) k_update_xr(Grid g, R* __restrict__ x, R* __restrict__ r,
-                                                   const R* __restrict__ p,
-                                                   const R* __restrict__ q,
-                                                   const double* __restrict__ rz,
-                                                   const double* __restrict__ pq, double* acc) {
-    __shared__ R sm[32];
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    const R alpha = (R)(*rz / *pq);
+__global__ void __launch_bounds__(RB) k_update_xr(Grid g, R* __restrict__ x, R* __restrict__ r,
+                                                  const R* __restrict__ p,
+                                                  const R* __restrict__ q,
+                                                  const double* __restrict__ rz,
+                                                  const double* __restrict__ pq, int first,
+                                                  double* acc) {
+    __shared__ R salpha;
+    if (threadIdx.x == 0) salpha = (R)(*rz / *pq);
+    __syncthreads();
+    const R alpha = salpha;
     R d = 0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+    ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
-        x[n] += alpha * p[n];
+        x[n] = first ? alpha * p[n] : x[n] + alpha * p[n];
         const R rn = r[n] - alpha * q[n];
         r[n] = rn;
-        d = rn * rn;
+        d += rn * rn;
     }
-    d = block_sum(d, sm);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicAdd(acc, (double)d);
+    block_add(d, acc);
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_dot(Grid g, const R* __restrict__ a,
-                                             const R* __restrict__ b, double* acc) {
-    __shared__ R sm[32];
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+__global__ void __launch_bounds__(RB) k_dot(Grid g, const R* __restrict__ a,
+                                            const R* __restrict__ b, double* acc) {
     R d = 0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+    ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
-        d = a[n] * b[n];
+        d += a[n] * b[n];
     }
-    d = block_sum(d, sm);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicAdd(acc, (double)d);
-}
-
-// p = z + beta p, beta = rz_new / rz_old (beta = 0 when first)
-template <typename R>
-__global__ void k_update_p(Grid g, R* __restrict__ p, const R* __restrict__ z,
-                           const double* __restrict__ rz_new, const double* __restrict__ rz_old,
-                           int first) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
-    const R beta = first ? (R)0 : (R)(*rz_new / *rz_old);
-    p[n] = z[n] + beta * p[n];
-}
-
-template <typename R>
-__global__ void k_zero_interior(Grid g, R* __restrict__ x) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    x[g.at(i, j, k)] = 0;
+    block_add(d, acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -363,8 +397,9 @@ static int alloc_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
     int nlev = 0;
     while (true) {
         Level<R>& L = H.lv[nlev];
+        L = Level<R>();
         L.g = g;
-        R** arrs[5] = {&L.cx, &L.cy, &L.cz, &L.diag, &L.idiag};
+        R** arrs[6] = {&L.cx, &L.cy, &L.cz, &L.diag, &L.idiag, &L.xs};
         for (auto a : arrs) {
             int rc = dev_alloc(h, (void**)a, sizeof(R) * g.total);
             if (rc) return rc;
@@ -379,7 +414,7 @@ static int alloc_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
         g = make_grid((g.nx + 1) / 2, (g.ny + 1) / 2, (g.nz + 1) / 2);
     }
     H.nlev = nlev;
-    R** vecs[5] = {&H.x, &H.r, &H.z, &H.p, &H.q};
+    R** vecs[6] = {&H.x, &H.r, &H.z, &H.p, &H.p2, &H.q};
     for (auto a : vecs) {
         int rc = dev_alloc(h, (void**)a, sizeof(R) * h->g.total);
         if (rc) return rc;
@@ -394,9 +429,10 @@ static void free_hierarchy(Hierarchy<R>& H) {
     for (int l = 0; l < H.nlev; ++l) {
         Level<R>& L = H.lv[l];
         cudaFree(L.cx); cudaFree(L.cy); cudaFree(L.cz); cudaFree(L.diag); cudaFree(L.idiag);
+        cudaFree(L.xs);
         if (l > 0) { cudaFree(L.x); cudaFree(L.b); }
     }
-    cudaFree(H.x); cudaFree(H.r); cudaFree(H.z); cudaFree(H.p); cudaFree(H.q);
+    cudaFree(H.x); cudaFree(H.r); cudaFree(H.z); cudaFree(H.p); cudaFree(H.p2); cudaFree(H.q);
     H = Hierarchy<R>();
 }
 
@@ -404,7 +440,7 @@ template <typename R>
 static int build_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
     const Grid& g = h->g;
     Level<R>& L0 = H.lv[0];
-    WPF_LAUNCH(h, KC_COEF, k_l0_coeffs<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, h->stream>>>(
+    WPF_LAUNCH(h, KC_COEF, k_l0_coeffs<R><<<row_blocks(h, g), RB, 0, h->stream>>>(
         g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag));
     for (int l = 0; l + 1 < H.nlev; ++l) {
         Level<R>& F = H.lv[l];
@@ -416,17 +452,19 @@ static int build_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
     return WPF_OK;
 }
 
-template <typename R>
-static void rbgs_grid(const Grid& g, dim3& gr, dim3& b) {
-    b = cell_block();
-    const int half = (g.nx + 1) / 2;
-    gr = dim3((half + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
+static dim3 sweep_grid(const Grid& g) {
+    return dim3((g.nx + SX - 1) / SX, (g.ny + SY - 1) / SY, (g.nz + SZC - 1) / SZC);
 }
 
-// One V-cycle z = M r (level 0 aliases b = r, x = z).
+// One V-cycle z = M r (level 0 aliases b = r, x = z); rz != null accumulates
+// r.z in the last level-0 sweep.  Sweeps alternate between the two buffers of
+// a level so that the 2*nu sweeps end in the level's output buffer x: the
+// first pre-sweep writes xs, the last post-sweep writes x.
 template <typename R>
-static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu) {
+static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu, double* rz) {
     cudaStream_t s = h->stream;
+    const dim3 sb(SX, SY);
+    const R* pre_end[MAX_LEVELS];
     for (int l = 0; l < H.nlev; ++l) {
         Level<R>& L = H.lv[l];
         const Grid& g = L.g;
@@ -434,28 +472,33 @@ static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu) {
             WPF_LAUNCH(h, KC_MGREST, k_coarse_solve<R><<<1, 256, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 16));
             break;
         }
-        dim3 b, gr;
-        rbgs_grid<R>(g, gr, b);
-        WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b));
-        WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
-        for (int it = 1; it < nu; ++it) {
-            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
-            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+        const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
+        R* buf[2] = {L.xs, L.x};
+        for (int it = 0; it < nu; ++it) {
+            const R* in = buf[(it + 1) & 1];
+            R* out = buf[it & 1];
+            WPF_LAUNCH(h, cls, k_sweep<R><<<sweep_grid(g), sb, 0, s>>>(
+                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, it == 0, nullptr, g, nullptr));
         }
+        pre_end[l] = buf[(nu - 1) & 1];
         Level<R>& C = H.lv[l + 1];
         WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
-            g, C.g, L.cx, L.cy, L.cz, L.diag, L.x, L.b, C.b, C.x));
+            g, C.g, L.cx, L.cy, L.cz, L.diag, pre_end[l], L.b, C.b));
     }
     for (int l = H.nlev - 2; l >= 0; --l) {
         Level<R>& L = H.lv[l];
         Level<R>& C = H.lv[l + 1];
         const Grid& g = L.g;
-        WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x));
-        dim3 b, gr;
-        rbgs_grid<R>(g, gr, b);
+        const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
+        R* buf[2] = {L.xs, L.x};
         for (int it = 0; it < nu; ++it) {
-            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
-            WPF_LAUNCH(h, (l == 0 ? KC_SMOOTH0 : KC_MGREST), k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+            const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
+            const R* in = buf[(w + 1) & 1];
+            R* out = buf[w & 1];
+            const bool last0 = (l == 0 && it == nu - 1);
+            WPF_LAUNCH(h, cls, k_sweep<R><<<sweep_grid(g), sb, 0, s>>>(
+                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, 0, it == 0 ? C.x : nullptr, C.g,
+                last0 ? rz : nullptr));
         }
     }
 }
@@ -469,33 +512,34 @@ static int read_slot(wpf_handle* h, int slot, int n = 1) {
 }
 
 // PCG on A' e = r (H.r holds r on entry); e accumulates in H.x.  Stops when
-// ||r_k|| <= tol * ||r_0|| or after maxit iterations; returns iterations.
+// ||r_k|| <= tol * ||r_0|| or after maxit iterations.
 template <typename R>
 static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, int* iters,
                double* final_ratio) {
     const Grid& g = h->g;
     cudaStream_t s = h->stream;
-    dim3 gr = cell_grid(g.nx, g.ny, g.nz), b = cell_block();
+    const unsigned rb = row_blocks(h, g);
     Level<R>& L0 = H.lv[0];
     double* d = h->dsc;
-    WPF_LAUNCH(h, KC_VEC, k_zero_interior<R><<<gr, b, 0, s>>>(g, H.x));
-    WPF_CUDA(cudaMemsetAsync(d + S_RZ0, 0, 2 * sizeof(double), s));
-    WPF_CUDA(cudaMemsetAsync(d + S_RR, 0, sizeof(double), s));
-    WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.r, d + S_RR));
-    vcycle(h, H, nu);
-    WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0));
-    WPF_LAUNCH(h, KC_VEC, k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0, d + S_RZ0, 1));
+    WPF_CUDA(cudaMemsetAsync(d + S_PQ, 0, 4 * sizeof(double), s));   // PQ, RR, RZ0, RZ1
+    WPF_LAUNCH(h, KC_VEC, k_dot<R><<<rb, RB, 0, s>>>(g, H.r, H.r, d + S_RR));
     int rc = read_slot(h, S_RR);
     if (rc) return rc;
     const double r0 = sqrt(h->hsc[S_RR]);
     *iters = 0;
     *final_ratio = 1.0;
     if (!(r0 > 0.0)) return r0 == 0.0 ? WPF_OK : WPF_ERR_NONFINITE;
-    int cur = 0;
+    vcycle(h, H, nu, d + S_RZ0);
+    int cur = 0;          // rz of this iteration in S_RZ0 + cur
+    R* pold = H.p2;
+    R* pnew = H.p;
     for (int it = 0; it < maxit; ++it) {
         WPF_CUDA(cudaMemsetAsync(d + S_PQ, 0, 2 * sizeof(double), s));   // S_PQ, S_RR
-        WPF_LAUNCH(h, KC_APPLY, k_apply_dot<R><<<gr, b, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.p, H.q, d + S_PQ));
-        WPF_LAUNCH(h, KC_VEC, k_update_xr<R><<<gr, b, 0, s>>>(g, H.x, H.r, H.p, H.q, d + S_RZ0 + cur, d + S_PQ, d + S_RR));
+        WPF_LAUNCH(h, KC_APPLY, k_apply_p<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.z, pold, pnew,
+                                                 H.q, d + S_RZ0 + cur, d + S_RZ0 + (cur ^ 1),
+                                                 it == 0, d + S_PQ));
+        WPF_LAUNCH(h, KC_VEC, k_update_xr<R><<<rb, RB, 0, s>>>(g, H.x, H.r, pnew, H.q, d + S_RZ0 + cur, d + S_PQ,
+                                                   it == 0, d + S_RR));
         rc = read_slot(h, S_PQ, 2);
         if (rc) return rc;
         *iters = it + 1;
@@ -503,12 +547,11 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
         *final_ratio = rn / r0;
         if (!(rn == rn) || isinf(rn)) return WPF_ERR_NONFINITE;
         if (rn <= tol * r0) return WPF_OK;
-        vcycle(h, H, nu);
         const int nxt = cur ^ 1;
         WPF_CUDA(cudaMemsetAsync(d + S_RZ0 + nxt, 0, sizeof(double), s));
-        WPF_LAUNCH(h, KC_VEC, k_dot<R><<<gr, b, 0, s>>>(g, H.r, H.z, d + S_RZ0 + nxt));
-        WPF_LAUNCH(h, KC_VEC, k_update_p<R><<<gr, b, 0, s>>>(g, H.p, H.z, d + S_RZ0 + nxt, d + S_RZ0 + cur, 0));
+        vcycle(h, H, nu, d + S_RZ0 + nxt);
         cur = nxt;
+        R* t = pold; pold = pnew; pnew = t;
     }
     return WPF_ERR_NOT_CONVERGED;
 }
@@ -535,7 +578,7 @@ template <typename R>
 static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     const Grid& g = h->g;
     cudaStream_t s = h->stream;
-    dim3 gr = cell_grid(g.nx, g.ny, g.nz), b = cell_block();
+    const unsigned rb = row_blocks(h, g);
     const bool mixed = h->opts.mode == WPF_SOLVER_MIXED;
     int rc = build_hierarchy(h, H);
     if (rc) return rc;
@@ -544,8 +587,8 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     double relres = 0.0, bnorm = 0.0, relres0 = 0.0;
     for (int pass = 0; pass <= h->opts.max_outer; ++pass) {
         WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 2 * sizeof(double), s));
-        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<gr, b, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm,
-                                      H.r, h->dsc, pass == 0));
+        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+                                                          h->flags, h->qterm, H.r, h->dsc, pass == 0));
         WPF_CUDA(cudaGetLastError());
         rc = read_slot(h, S_RR64, 2);
         if (rc) return rc;
@@ -564,7 +607,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         rc = pcg<R>(h, H, tol, h->opts.max_inner, nu, &its, &ratio);
         inner_total += its;
         if (rc == WPF_ERR_NONFINITE) { status = rc; break; }
-        WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<gr, b, 0, s>>>(g, h->pressure, H.x));
+        WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x));
         WPF_CUDA(cudaGetLastError());
     }
     if (st) {
