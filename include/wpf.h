@@ -77,7 +77,9 @@ typedef struct wpf_solver_opts {
     int32_t max_inner;         /* PCG iterations per pass (default 500)                */
     int32_t smooth_sweeps;     /* red-black Gauss-Seidel sweeps per V-cycle side (2)   */
     double rtol;               /* ||b - A p|| <= rtol * ||b|| (true FP64 residual)      */
-    double inner_rtol;         /* inner PCG reduction per pass in MIXED mode (1e-5)    */
+    double inner_rtol;         /* inner PCG reduction per pass in MIXED mode (1e-4)    */
+    int64_t sweep_min_cells;   /* levels with at least this many cells use the pipelined
+                                  one-pass sweep kernel (0 = default 2^20)              */
 } wpf_solver_opts;
 
 /* Per-step / per-solve statistics. */

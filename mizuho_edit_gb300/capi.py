@@ -47,7 +47,8 @@ class Well(C.Structure):
 
 class SolverOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_outer", C.c_int32), ("max_inner", C.c_int32),
-                ("smooth_sweeps", C.c_int32), ("rtol", C.c_double), ("inner_rtol", C.c_double)]
+                ("smooth_sweeps", C.c_int32), ("rtol", C.c_double), ("inner_rtol", C.c_double),
+                ("sweep_min_cells", C.c_int64)]
 
 
 class StepStats(C.Structure):

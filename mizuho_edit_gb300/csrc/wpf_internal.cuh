@@ -266,19 +266,20 @@ __device__ __forceinline__ T block_max(T v, T* sm, T ident) {
 // (coalesced), and each block issues one atomic per reduced quantity.
 constexpr int RB = 256;
 
+// A block's 8 warps take a 4 (y) x 2 (z) patch of rows, so the y and z
+// neighbours of a warp's row are mostly rows of the same block (L1 reuse).
 #define ROW_LOOP(g)                                                                        \
-    const long long nrows_ = (long long)(g).ny * (g).nz;                                   \
-    const int lane_ = threadIdx.x & 31;                                                    \
-    for (long long t_ = blockIdx.x * (long long)(RB / 32) + (threadIdx.x >> 5); t_ < nrows_; \
-         t_ += (long long)gridDim.x * (RB / 32))                                           \
-        for (int i = 1 + lane_, j = 1 + (int)(t_ % (g).ny), k = 1 + (int)(t_ / (g).ny);    \
+    const int nby_ = ((g).ny + 3) >> 2, npatch_ = nby_ * (((g).nz + 1) >> 1);             \
+    const int lane_ = threadIdx.x & 31, wy_ = (threadIdx.x >> 5) & 3, wz_ = threadIdx.x >> 7; \
+    for (int t_ = blockIdx.x; t_ < npatch_; t_ += gridDim.x)                               \
+        for (int k = 1 + (t_ / nby_) * 2 + wz_, j = 1 + (t_ % nby_) * 4 + wy_,             \
+                 i = (j <= (g).ny && k <= (g).nz) ? 1 + lane_ : (g).nx + 1;                \
              i <= (g).nx; i += 32)
 
 inline unsigned row_blocks(const wpf_handle* h, const Grid& g, int per_sm = 8) {
-    const long long rows = (long long)g.ny * g.nz;
-    long long b = (rows + RB / 32 - 1) / (RB / 32);
+    const long long patches = (long long)((g.ny + 3) / 4) * ((g.nz + 1) / 2);
     const long long cap = (long long)h->nsm * per_sm;
-    return (unsigned)(b < cap ? b : cap);
+    return (unsigned)(patches < cap ? patches : cap);
 }
 
 template <typename T>

@@ -27,14 +27,16 @@
 // Dead cells (Dirichlet, or aggregates of only Dirichlet cells) carry a zero
 // diagonal and zero couplings and never change.
 //
-// One red-black sweep is one kernel (k_sweep): each block owns a 32x8 column
-// of cells and a 32-plane chunk of z, keeps a four-plane ring of x in shared
-// memory and marches up in z, updating the first colour of plane k+1 and then
-// the second colour of plane k.  The first colour is recomputed on a one-cell
+// On the large levels one red-black sweep is one kernel (k_sweep_async): each
+// block owns a 32x8 column of cells and a 32-plane chunk of z and marches up
+// in z, updating the first colour of plane k+1 and then the second colour of
+// plane k, with the planes' x, couplings, 1/diag and b staged in shared memory
+// by cp.async two planes ahead.  The first colour is recomputed on a one-cell
 // ring around the tile from the old values (it depends on old values only),
 // so every block produces exactly the two-kernel red-black result; the sweep
 // reads x from one buffer and writes the other, so no block can see another
-// block's new values.
+// block's new values.  Mid-size levels use in-place two-kernel half-sweeps and
+// the levels of at most 4096 cells run their whole sub-cycle in one block.
 #include <math.h>
 #include <stdio.h>
 
@@ -176,97 +178,210 @@ __device__ __forceinline__ R offsum(const R* __restrict__ cx, const R* __restric
 }
 
 // ---------------------------------------------------------------------------
-// One full red-black Gauss-Seidel sweep (first colour c0, then 1-c0) from
-// xin to xout.  zero_init: xin is taken as zero (first pre-smoothing sweep).
-// xc != null: the coarse correction x_{l+1}(parent) is added to every old
-// value as it is loaded (prolongation fused into the first post sweep).
-// dot != null: accumulate b.xout (the PCG r.z, level 0 only).
+// Pipelined red-black sweep for the large levels.  Block = 32x8 threads, tile
+// = 32x8 cells of a plane, z chunk of SZC planes.  Shared memory holds NSLOT
+// plane slots; each slot carries x on the tile + 2-cell ring and the
+// couplings / 1/diag / b on the tile + 1-cell ring, filled by cp.async
+// (4- or 8-byte async copies, zero-filled outside the halo box) two planes
+// ahead of use, so the compute phases read only shared memory.
 // ---------------------------------------------------------------------------
+constexpr int NSLOT = 6;
+constexpr int R1X = SX + 2, R1Y = SY + 2;   // first-colour region: tile + 1-cell ring
+
 template <typename R>
-__global__ void __launch_bounds__(SX * SY) k_sweep(Grid g, const R* __restrict__ cx,
-                                                   const R* __restrict__ cy,
-                                                   const R* __restrict__ cz,
-                                                   const R* __restrict__ idiag,
-                                                   const R* __restrict__ b,
-                                                   const R* __restrict__ xin, R* __restrict__ xout,
-                                                   int c0, int zero_init, const R* __restrict__ xc,
-                                                   Grid gc, double* dot) {
-    __shared__ R xs[4][FY][FX];
+struct SweepSlot {
+    R x[FY][FX];             // i in [i0-2, i0+33], j in [j0-2, j0+9]
+    R cx[R1Y][R1X + 1];      // i in [i0-2, i0+32], j in [j0-1, j0+8]
+    R cy[R1Y + 1][R1X];      // i in [i0-1, i0+32], j in [j0-2, j0+8]
+    R cz[R1Y][R1X];          // region R1: i in [i0-1, i0+32], j in [j0-1, j0+8]
+    R id[R1Y][R1X];
+    R b[R1Y][R1X];
+};
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool ok) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(ok ? 4 : 0));
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool ok) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(ok ? 8 : 0));
+}
+template <typename R>
+__device__ __forceinline__ void cp_async_el(R* smem, const R* gmem, bool ok) {
+    if (sizeof(R) == 4) cp_async4(smem, gmem, ok);
+    else cp_async8(smem, gmem, ok);
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// ZERO: xin is zero (first pre-smoothing sweep).  xc != null: prolongation
+// x += x_{l+1}(parent) fused into the loads.  dot != null: accumulate b.xout.
+template <typename R, bool ZERO>
+__global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __restrict__ cx,
+                                                         const R* __restrict__ cy,
+                                                         const R* __restrict__ cz,
+                                                         const R* __restrict__ idiag,
+                                                         const R* __restrict__ b,
+                                                         const R* __restrict__ xin,
+                                                         R* __restrict__ xout, int c0,
+                                                         const R* __restrict__ xc, Grid gc,
+                                                         double* dot) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SweepSlot<R>* slots = reinterpret_cast<SweepSlot<R>*>(smem_raw);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * SX + tx;
+    constexpr int NT = SX * SY;
     const int i0 = 1 + blockIdx.x * SX, j0 = 1 + blockIdx.y * SY;
     const int k0 = 1 + blockIdx.z * SZC;
     const int k1 = min(g.nz, k0 + SZC - 1);
-    const long long sy = g.P, sz = g.S;
     R dacc = 0;
-
-    auto load_plane = [&](int k) {
-        R(*P)[FX] = xs[k & 3];
-        for (int q = tid; q < FX * FY; q += SX * SY) {
-            const int fj = q / FX, fi = q - fj * FX;
-            const int i = i0 - 2 + fi, j = j0 - 2 + fj;
-            R v = 0;
-            if (!zero_init && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz) {
-                v = xin[g.at(i, j, k)];
-                if (xc) v += xc[gc.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+    auto slot = [&](int k) -> SweepSlot<R>& { return slots[(k + 2 * NSLOT) % NSLOT]; };
+    // inside the allocated halo box (values there are the array's: 0 on halos)
+    auto inbox = [&](int i, int j, int k) {
+        return i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1;
+    };
+    auto interior = [&](int i, int j, int k) {
+        return i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz;
+    };
+    auto issue = [&](int k) {
+        SweepSlot<R>& S = slot(k);
+        for (int q = tid; q < FX * FY; q += NT) {
+            const int fj = q / FX, fi = q - fj * FX, i = i0 - 2 + fi, j = j0 - 2 + fj;
+            if (ZERO) {
+                S.x[fj][fi] = 0;   // old x is zero; halo / ring entries must read as 0
+            } else {
+                const bool ok = inbox(i, j, k);
+                cp_async_el(&S.x[fj][fi], ok ? xin + g.at(i, j, k) : xin, ok);
             }
-            P[fj][fi] = v;
+        }
+        for (int q = tid; q < R1Y * (R1X + 1); q += NT) {
+            const int c = q / (R1X + 1), a = q - c * (R1X + 1), i = i0 - 2 + a, j = j0 - 1 + c;
+            const bool ok = inbox(i, j, k);
+            cp_async_el(&S.cx[c][a], ok ? cx + g.at(i, j, k) : cx, ok);
+        }
+        for (int q = tid; q < (R1Y + 1) * R1X; q += NT) {
+            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 2 + c;
+            const bool ok = inbox(i, j, k);
+            cp_async_el(&S.cy[c][a], ok ? cy + g.at(i, j, k) : cy, ok);
+        }
+        for (int q = tid; q < R1Y * R1X; q += NT) {
+            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 1 + c;
+            const bool ok = inbox(i, j, k);
+            const long long n = ok ? g.at(i, j, k) : 0;
+            cp_async_el(&S.cz[c][a], cz + n, ok);
+            cp_async_el(&S.id[c][a], idiag + n, ok);
+            cp_async_el(&S.b[c][a], b + n, ok);
+        }
+        cp_async_commit();
+    };
+    // after the slot of plane k has landed: add the coarse correction to the
+    // x values this thread copied (its own cp.async results are visible to it)
+    auto correct = [&](int k) {
+        if (ZERO || !xc) return;
+        SweepSlot<R>& S = slot(k);
+        for (int q = tid; q < FX * FY; q += NT) {
+            const int fj = q / FX, fi = q - fj * FX, i = i0 - 2 + fi, j = j0 - 2 + fj;
+            if (interior(i, j, k)) S.x[fj][fi] += xc[gc.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
         }
     };
-    // first colour of plane k on the tile and its one-cell ring, in place
     auto first_colour = [&](int k) {
         if (k < 1 || k > g.nz) return;
-        R(*P)[FX] = xs[k & 3];
-        R(*Pm)[FX] = xs[(k - 1) & 3];
-        R(*Pp)[FX] = xs[(k + 1) & 3];
-        for (int q = tid; q < (FX - 2) * (FY - 2); q += SX * SY) {
-            const int fj = 1 + q / (FX - 2), fi = 1 + q % (FX - 2);
-            const int i = i0 - 2 + fi, j = j0 - 2 + fj;
+        SweepSlot<R>& S = slot(k);
+        const SweepSlot<R>& Sm = slot(k - 1);
+        const SweepSlot<R>& Sp = slot(k + 1);
+        for (int q = tid; q < R1Y * R1X; q += NT) {
+            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 1 + c;
             if (i < 1 || i > g.nx || j < 1 || j > g.ny || ((i + j + k) & 1) != c0) continue;
-            const long long n = g.at(i, j, k);
-            const R s = b[n] + cx[n] * P[fj][fi + 1] + cx[n - 1] * P[fj][fi - 1] +
-                        cy[n] * P[fj + 1][fi] + cy[n - sy] * P[fj - 1][fi] + cz[n] * Pp[fj][fi] +
-                        cz[n - sz] * Pm[fj][fi];
-            P[fj][fi] = idiag[n] * s;
+            R s = S.b[c][a];
+            if (!ZERO)
+                s += S.cx[c][a + 1] * S.x[c + 1][a + 2] + S.cx[c][a] * S.x[c + 1][a] +
+                     S.cy[c + 1][a] * S.x[c + 2][a + 1] + S.cy[c][a] * S.x[c][a + 1] +
+                     S.cz[c][a] * Sp.x[c + 1][a + 1] + Sm.cz[c][a] * Sm.x[c + 1][a + 1];
+            S.x[c + 1][a + 1] = S.id[c][a] * s;
         }
     };
-    // second colour of plane k on the tile; writes both colours of the tile
     auto second_colour = [&](int k) {
-        R(*P)[FX] = xs[k & 3];
-        R(*Pm)[FX] = xs[(k - 1) & 3];
-        R(*Pp)[FX] = xs[(k + 1) & 3];
-        const int i = i0 + tx, j = j0 + ty, fi = tx + 2, fj = ty + 2;
+        const SweepSlot<R>& S = slot(k);
+        const SweepSlot<R>& Sm = slot(k - 1);
+        const SweepSlot<R>& Sp = slot(k + 1);
+        const int a = tx + 1, c = ty + 1, i = i0 + tx, j = j0 + ty;
         if (i <= g.nx && j <= g.ny) {
-            const long long n = g.at(i, j, k);
-            R v = P[fj][fi];
+            R v = S.x[c + 1][a + 1];
             if (((i + j + k) & 1) != c0) {
-                const R s = b[n] + cx[n] * P[fj][fi + 1] + cx[n - 1] * P[fj][fi - 1] +
-                            cy[n] * P[fj + 1][fi] + cy[n - sy] * P[fj - 1][fi] + cz[n] * Pp[fj][fi] +
-                            cz[n - sz] * Pm[fj][fi];
-                v = idiag[n] * s;
+                const R s = S.b[c][a] + S.cx[c][a + 1] * S.x[c + 1][a + 2] +
+                            S.cx[c][a] * S.x[c + 1][a] + S.cy[c + 1][a] * S.x[c + 2][a + 1] +
+                            S.cy[c][a] * S.x[c][a + 1] + S.cz[c][a] * Sp.x[c + 1][a + 1] +
+                            Sm.cz[c][a] * Sm.x[c + 1][a + 1];
+                v = S.id[c][a] * s;
             }
-            xout[n] = v;
-            if (dot) dacc += b[n] * v;
+            xout[g.at(i, j, k)] = v;
+            if (dot) dacc += S.b[c][a] * v;
         }
     };
 
-    load_plane(k0 - 2);
-    load_plane(k0 - 1);
-    load_plane(k0);
+    for (int k = k0 - 2; k <= k0 + 3; ++k) issue(k);
+    cp_async_wait<2>();                       // planes k0-2 .. k0+1 landed
+    for (int k = k0 - 2; k <= k0 + 1; ++k) correct(k);
     __syncthreads();
     first_colour(k0 - 1);
     __syncthreads();
-    load_plane(k0 + 1);
-    __syncthreads();
     first_colour(k0);
     for (int k = k0; k <= k1; ++k) {
-        __syncthreads();           // slot (k+2)&3 held plane k-2, read by the previous step
-        load_plane(k + 2);
+        __syncthreads();                      // the slot of plane k+4 held plane k-2
+        issue(k + 4);
+        cp_async_wait<2>();                   // plane k+2 landed
+        correct(k + 2);
         __syncthreads();
         first_colour(k + 1);
         __syncthreads();
         second_colour(k);
     }
+    cp_async_wait<0>();
     if (dot) block_add(dacc, dot);
+}
+
+template <typename R>
+constexpr size_t sweep_smem() { return sizeof(SweepSlot<R>) * NSLOT; }
+
+// One colour of red-black Gauss-Seidel in place (mid-size levels).  Thread
+// (t,j,k) handles the cell of colour `color` at i = 1 + 2t + ((color+1+j+k) & 1).
+template <typename R>
+__global__ void k_rbgs(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
+                       const R* __restrict__ cz, const R* __restrict__ idiag, R* __restrict__ x,
+                       const R* __restrict__ b, int color) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    const int i = 1 + 2 * t + ((color + 1 + j + k) & 1);
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    x[n] = idiag[n] * (b[n] + offsum(cx, cy, cz, x, n, g.P, g.S));
+}
+
+// First red sweep from a zero initial guess: red cells get idiag*b, black 0.
+template <typename R>
+__global__ void k_rbgs_first(Grid g, const R* __restrict__ idiag, R* __restrict__ x,
+                             const R* __restrict__ b) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long n = g.at(i, j, k);
+    x[n] = ((i + j + k) & 1) ? (R)0 : idiag[n] * b[n];
+}
+
+// x_l += x_{l+1}(parent) on live cells.
+template <typename R>
+__global__ void k_prolong(Grid f, Grid c, const R* __restrict__ idiag, R* __restrict__ x,
+                          const R* __restrict__ xc) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > f.nx || j > f.ny || k > f.nz) return;
+    const long long n = f.at(i, j, k);
+    if (idiag[n] != (R)0) x[n] += xc[c.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
 }
 
 // Residual of level l restricted (summed over the aggregate) into b of level l+1.
@@ -297,27 +412,87 @@ __global__ void k_resid_restrict(Grid f, Grid c, const R* __restrict__ cx, const
     bc[c.at(I, J, K)] = s;
 }
 
-// Coarsest level: Gauss-Seidel sweeps in one block from x = 0.
+// Levels with at most BOTTOM_CELLS cells: the whole sub-V-cycle (same
+// smoother, restriction and prolongation as above) in one block.
+constexpr int BOTTOM_CELLS = 4096;
+constexpr int BOTTOM_THREADS = 1024;
+
 template <typename R>
-__global__ void k_coarse_solve(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
-                               const R* __restrict__ cz, const R* __restrict__ idiag,
-                               R* __restrict__ x, const R* __restrict__ b, int sweeps) {
-    const int ncell = g.nx * g.ny * g.nz;
-    for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-        const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
-        x[g.at(i, j, k)] = 0;
-    }
-    __syncthreads();
-    for (int s = 0; s < sweeps; ++s)
-        for (int color = 0; color < 2; ++color) {
-            for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-                const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
-                if (((i + j + k) & 1) != color) continue;
-                const long long n = g.at(i, j, k);
-                x[n] = idiag[n] * (b[n] + offsum(cx, cy, cz, x, n, g.P, g.S));
-            }
-            __syncthreads();
+struct BottomArgs {
+    int l0, nlev, nu;
+    Level<R> lv[MAX_LEVELS];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(BottomArgs<R> A) {
+    const int T = blockDim.x;
+    auto colour_sweep = [&](const Level<R>& L, int color) {
+        const Grid& g = L.g;
+        const int nc = g.nx * g.ny * g.nz;
+        for (int q = threadIdx.x; q < nc; q += T) {
+            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
+            if (((i + j + k) & 1) != color) continue;
+            const long long n = g.at(i, j, k);
+            L.x[n] = L.idiag[n] * (L.b[n] + offsum(L.cx, L.cy, L.cz, L.x, n, g.P, g.S));
         }
+        __syncthreads();
+    };
+    auto zero_x = [&](const Level<R>& L) {
+        const Grid& g = L.g;
+        const int nc = g.nx * g.ny * g.nz;
+        for (int q = threadIdx.x; q < nc; q += T) {
+            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
+            L.x[g.at(i, j, k)] = 0;
+        }
+        __syncthreads();
+    };
+    const int last = A.nlev - 1;
+    for (int l = A.l0; l <= last; ++l) {
+        const Level<R>& L = A.lv[l];
+        zero_x(L);
+        if (l == last) {
+            for (int s = 0; s < 16; ++s) { colour_sweep(L, 0); colour_sweep(L, 1); }
+            break;
+        }
+        for (int s = 0; s < A.nu; ++s) { colour_sweep(L, 0); colour_sweep(L, 1); }
+        const Level<R>& C = A.lv[l + 1];
+        const Grid& f = L.g;
+        const Grid& c = C.g;
+        const int ncc = c.nx * c.ny * c.nz;
+        for (int q = threadIdx.x; q < ncc; q += T) {
+            const int I = 1 + q % c.nx, J = 1 + (q / c.nx) % c.ny, K = 1 + q / (c.nx * c.ny);
+            R s = 0;
+            for (int dk = 0; dk < 2; ++dk) {
+                const int k = 2 * K - 1 + dk;
+                if (k > f.nz) break;
+                for (int dj = 0; dj < 2; ++dj) {
+                    const int j = 2 * J - 1 + dj;
+                    if (j > f.ny) break;
+                    for (int di = 0; di < 2; ++di) {
+                        const int i = 2 * I - 1 + di;
+                        if (i > f.nx) break;
+                        const long long n = f.at(i, j, k);
+                        s += L.b[n] - (L.diag[n] * L.x[n] - offsum(L.cx, L.cy, L.cz, L.x, n, f.P, f.S));
+                    }
+                }
+            }
+            C.b[c.at(I, J, K)] = s;
+        }
+        __syncthreads();
+    }
+    for (int l = last - 1; l >= A.l0; --l) {
+        const Level<R>& L = A.lv[l];
+        const Level<R>& C = A.lv[l + 1];
+        const Grid& g = L.g;
+        const int nc = g.nx * g.ny * g.nz;
+        for (int q = threadIdx.x; q < nc; q += T) {
+            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
+            const long long n = g.at(i, j, k);
+            if (L.idiag[n] != (R)0) L.x[n] += C.x[C.g.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+        }
+        __syncthreads();
+        for (int s = 0; s < A.nu; ++s) { colour_sweep(L, 1); colour_sweep(L, 0); }
+    }
 }
 
 // ---- PCG vector kernels (persistent row loops, one atomic per block) -------
@@ -456,50 +631,101 @@ static dim3 sweep_grid(const Grid& g) {
     return dim3((g.nx + SX - 1) / SX, (g.ny + SY - 1) / SY, (g.nz + SZC - 1) / SZC);
 }
 
+template <typename R>
+static void rbgs_grid(const Grid& g, dim3& gr, dim3& b) {
+    b = cell_block();
+    const int half = (g.nx + 1) / 2;
+    gr = dim3((half + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
+}
+
+static long long ncells(const Grid& g) { return (long long)g.nx * g.ny * g.nz; }
+constexpr long long BIG_CELLS = 1LL << 20;   // default: levels swept by the pipelined kernel
+
 // One V-cycle z = M r (level 0 aliases b = r, x = z); rz != null accumulates
-// r.z in the last level-0 sweep.  Sweeps alternate between the two buffers of
-// a level so that the 2*nu sweeps end in the level's output buffer x: the
-// first pre-sweep writes xs, the last post-sweep writes x.
+// r.z (in the last level-0 sweep when that level is a big one, else by a dot).
+// Big levels sweep between their two buffers so that the 2*nu sweeps end in
+// the level's output buffer x (the first pre-sweep writes xs, the last
+// post-sweep writes x); mid levels sweep x in place; the levels with at most
+// BOTTOM_CELLS cells run in one k_bottom block.
 template <typename R>
 static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu, double* rz) {
     cudaStream_t s = h->stream;
     const dim3 sb(SX, SY);
     const R* pre_end[MAX_LEVELS];
-    for (int l = 0; l < H.nlev; ++l) {
+    const long long big = h->opts.sweep_min_cells > 0 ? h->opts.sweep_min_cells : BIG_CELLS;
+    int lb = H.nlev - 1;
+    while (lb > 0 && ncells(H.lv[lb - 1].g) <= BOTTOM_CELLS) --lb;
+    for (int l = 0; l < lb; ++l) {
         Level<R>& L = H.lv[l];
         const Grid& g = L.g;
-        if (l == H.nlev - 1) {
-            WPF_LAUNCH(h, KC_MGREST, k_coarse_solve<R><<<1, 256, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 16));
-            break;
-        }
         const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
-        R* buf[2] = {L.xs, L.x};
-        for (int it = 0; it < nu; ++it) {
-            const R* in = buf[(it + 1) & 1];
-            R* out = buf[it & 1];
-            WPF_LAUNCH(h, cls, k_sweep<R><<<sweep_grid(g), sb, 0, s>>>(
-                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, it == 0, nullptr, g, nullptr));
+        if (ncells(g) >= big) {
+            R* buf[2] = {L.xs, L.x};
+            for (int it = 0; it < nu; ++it) {
+                const R* in = buf[(it + 1) & 1];
+                R* out = buf[it & 1];
+                if (it == 0)
+                    WPF_LAUNCH(h, cls, k_sweep_async<R, true><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
+                        g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
+                else
+                    WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
+                        g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
+            }
+            pre_end[l] = buf[(nu - 1) & 1];
+        } else {
+            dim3 b, gr;
+            rbgs_grid<R>(g, gr, b);
+            WPF_LAUNCH(h, cls, k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b));
+            WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+            for (int it = 1; it < nu; ++it) {
+                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+            }
+            pre_end[l] = L.x;
         }
-        pre_end[l] = buf[(nu - 1) & 1];
         Level<R>& C = H.lv[l + 1];
         WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
             g, C.g, L.cx, L.cy, L.cz, L.diag, pre_end[l], L.b, C.b));
     }
-    for (int l = H.nlev - 2; l >= 0; --l) {
+    {
+        BottomArgs<R> A;
+        A.l0 = lb;
+        A.nlev = H.nlev;
+        A.nu = nu;
+        for (int l = 0; l < H.nlev; ++l) A.lv[l] = H.lv[l];
+        WPF_LAUNCH(h, lb == 0 ? KC_SMOOTH0 : KC_MGREST, k_bottom<R><<<1, BOTTOM_THREADS, 0, s>>>(A));
+    }
+    bool need_dot = rz != nullptr;
+    for (int l = lb - 1; l >= 0; --l) {
         Level<R>& L = H.lv[l];
         Level<R>& C = H.lv[l + 1];
         const Grid& g = L.g;
         const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
-        R* buf[2] = {L.xs, L.x};
-        for (int it = 0; it < nu; ++it) {
-            const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
-            const R* in = buf[(w + 1) & 1];
-            R* out = buf[w & 1];
-            const bool last0 = (l == 0 && it == nu - 1);
-            WPF_LAUNCH(h, cls, k_sweep<R><<<sweep_grid(g), sb, 0, s>>>(
-                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, 0, it == 0 ? C.x : nullptr, C.g,
-                last0 ? rz : nullptr));
+        if (ncells(g) >= big) {
+            R* buf[2] = {L.xs, L.x};
+            for (int it = 0; it < nu; ++it) {
+                const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
+                const R* in = buf[(w + 1) & 1];
+                R* out = buf[w & 1];
+                const bool last0 = (l == 0 && it == nu - 1 && rz);
+                if (last0) need_dot = false;
+                WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
+                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, it == 0 ? C.x : nullptr, C.g,
+                    last0 ? rz : nullptr));
+            }
+        } else {
+            dim3 b, gr;
+            rbgs_grid<R>(g, gr, b);
+            WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x));
+            for (int it = 0; it < nu; ++it) {
+                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+            }
         }
+    }
+    if (need_dot) {
+        const Grid& g = H.lv[0].g;
+        WPF_LAUNCH(h, KC_VEC, k_dot<R><<<row_blocks(h, g), RB, 0, s>>>(g, H.r, H.z, rz));
     }
 }
 
@@ -556,9 +782,20 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
     return WPF_ERR_NOT_CONVERGED;
 }
 
+template <typename R>
+static int set_sweep_smem() {
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sweep_smem<R>()));
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sweep_smem<R>()));
+    return WPF_OK;
+}
+
 int solver_setup(wpf_handle* h) {
+    int rc = h->opts.mode == WPF_SOLVER_MIXED ? set_sweep_smem<float>() : set_sweep_smem<double>();
+    if (rc) return rc;
     if (h->opts.mode == WPF_SOLVER_MIXED) {
-        int rc = alloc_hierarchy(h, h->h32);
+        rc = alloc_hierarchy(h, h->h32);
         if (rc) return rc;
         if (!h->r64) return dev_alloc(h, (void**)&h->r64, sizeof(double) * h->g.total);
         return WPF_OK;

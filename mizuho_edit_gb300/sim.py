@@ -33,7 +33,8 @@ class Simulation:
     def __init__(self, params: Params, permeab_rock: Optional[np.ndarray] = None,
                  phase: Optional[np.ndarray] = None, concent: Optional[np.ndarray] = None,
                  solver: str = "fp64", rtol: float = 1e-8, inner_rtol: float = 1e-4,
-                 max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2):
+                 max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2,
+                 sweep_min_cells: int = 0):
         self.L = capi.load()
         self.params = p = params
         if p.tfac is None:
@@ -49,7 +50,8 @@ class Simulation:
             ws[n] = capi.Well(w.ix, w.iy, w.iz, 0, w.pressure, w.injection, w.phase, w.concent)
         capi.check(self.L.wpf_set_wells(h, ws, len(p.wells)), "wpf_set_wells")
         self.set_solver(solver, rtol, inner_rtol=inner_rtol, max_inner=max_inner,
-                        max_outer=max_outer, smooth_sweeps=smooth_sweeps)
+                        max_outer=max_outer, smooth_sweeps=smooth_sweeps,
+                        sweep_min_cells=sweep_min_cells)
         # initial fields exactly as loadConfig builds them (wPFAW3D.f90:464-496)
         sh = self.halo_shape
         kr = np.full(sh, p.init_permeab, order="F")
@@ -96,9 +98,11 @@ class Simulation:
         return (p.nx + 2, p.ny + 2, p.nz + 2)
 
     def set_solver(self, mode: str = "fp64", rtol: float = 1e-8, inner_rtol: float = 1e-4,
-                   max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2):
+                   max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2,
+                   sweep_min_cells: int = 0):
         m = {"fp64": capi.SOLVER_FP64, "mixed": capi.SOLVER_MIXED}[mode]
-        o = capi.SolverOpts(m, max_outer, max_inner, smooth_sweeps, rtol, inner_rtol)
+        o = capi.SolverOpts(m, max_outer, max_inner, smooth_sweeps, rtol, inner_rtol,
+                            sweep_min_cells)
         capi.check(self.L.wpf_set_solver(self.h, C.byref(o)), "wpf_set_solver")
         self.solver = mode
 

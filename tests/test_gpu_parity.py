@@ -230,3 +230,45 @@ def test_not_converged_reported():
         with pytest.raises(capi.WpfError) as e:
             sim.solvePressure()
         assert e.value.status == capi.WPF_ERR_NOT_CONVERGED
+
+
+def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
+    """The one-pass pipelined red-black sweep (levels of >= 2^20 cells) gives
+    the same V-cycle as the two-kernel half-sweeps: same PCG iterations and
+    the same pressure to FP32 rounding."""
+    _, Simulation = _sim_mod()
+    case = _case((128, 128, 64), seed=21, log_var=2.0, corr_len=6.0)
+    p = case.params
+    out = {}
+    for name, thr in (("pipelined", 0), ("half", 1 << 40)):
+        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                        rtol=1e-10, sweep_min_cells=thr) as sim:
+            sim.calcPermeability()
+            st = sim.solvePressure()
+            assert st.converged and st.relres <= 1e-10
+            out[name] = (st.inner_iterations, sim.download("pressure"))
+    assert abs(out["pipelined"][0] - out["half"][0]) <= 1
+    assert rel_l2(out["pipelined"][1], out["half"][1]) < 1e-9
+
+
+@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+def test_large_solve_true_residual(oracle_mod, solver):
+    """At 2^20+ cells: the returned pressure satisfies the reference's own
+    assembled system (wPFAW3D.f90:629-936) to the requested relative residual."""
+    import scipy.sparse as sp
+    _, Simulation = _sim_mod()
+    case = _case((128, 96, 96), seed=22, log_var=2.0, corr_len=8.0)
+    p = case.params
+    ref = oracle_mod.OracleSim(p, case.permeab_rock, case.phase, case.concent)
+    ref.calcPermeability()
+    irn, jcn, val, b = ref.assemble()
+    N = p.nx * p.ny * p.nz
+    A = sp.csr_matrix((val, (irn, jcn)), shape=(N, N))
+    with Simulation(p, case.permeab_rock, case.phase, case.concent, solver=solver,
+                    rtol=1e-8) as sim:
+        sim.calcPermeability()
+        st = sim.solvePressure()
+        assert st.converged
+        x = sim.download("pressure")[1:-1, 1:-1, 1:-1].ravel(order="F")
+    res = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+    assert res <= 1.05e-8
