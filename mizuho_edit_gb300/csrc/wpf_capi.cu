@@ -103,6 +103,8 @@ static void free_all(wpf_handle* h) {
     for (double* p : d)
         if (p) cudaFree(p);
     if (h->flags) cudaFree(h->flags);
+    if (h->work) cudaFree(h->work);
+    if (h->dphys) cudaFree(h->dphys);
     if (h->dir_idx) cudaFree(h->dir_idx);
     solver_free(h);
     if (h->hsc) cudaFreeHost(h->hsc);
@@ -163,6 +165,10 @@ int wpf_create(const wpf_params* p, wpf_handle** out) {
     for (int a = 0; a < 9 && !rc; ++a) rc = dev_alloc(h, (void**)arrs[a], fb);
     if (!rc) rc = dev_alloc(h, (void**)&h->flags, h->g.total);
     if (!rc) rc = dev_alloc(h, (void**)&h->dsc, S_COUNT * sizeof(double));
+    if (!rc) rc = dev_alloc(h, (void**)&h->dphys, sizeof(Phys));
+    if (!rc && cudaMemcpyAsync(h->dphys, &h->phys, sizeof(Phys), cudaMemcpyHostToDevice, h->stream) !=
+                   cudaSuccess)
+        rc = WPF_ERR_CUDA;
     h->opts.mode = WPF_SOLVER_FP64;
     h->opts.max_outer = 20;
     h->opts.max_inner = 500;

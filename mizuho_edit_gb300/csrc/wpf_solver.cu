@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
 template <typename R>
 __global__ void __launch_bounds__(RB) k_add_correction(Grid g, double* __restrict__ pr,
                                                        const R* __restrict__ e) {
-    ROW_LOOP(g) {
+    ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         pr[n] += (double)e[n];
     }
@@ -185,40 +185,36 @@ __device__ __forceinline__ R offsum(const R* __restrict__ cx, const R* __restric
 // (4- or 8-byte async copies, zero-filled outside the halo box) two planes
 // ahead of use, so the compute phases read only shared memory.
 // ---------------------------------------------------------------------------
-constexpr int NSLOT = 6;
+constexpr int NSLOT = 7;
 constexpr int R1X = SX + 2, R1Y = SY + 2;   // first-colour region: tile + 1-cell ring
+constexpr int WX = SX + 8;                  // staged row: i in [i0-4, i0+SX+3], 16-byte aligned
 
 template <typename R>
 struct SweepSlot {
-    R x[FY][FX];             // i in [i0-2, i0+33], j in [j0-2, j0+9]
-    R cx[R1Y][R1X + 1];      // i in [i0-2, i0+32], j in [j0-1, j0+8]
-    R cy[R1Y + 1][R1X];      // i in [i0-1, i0+32], j in [j0-2, j0+8]
-    R cz[R1Y][R1X];          // region R1: i in [i0-1, i0+32], j in [j0-1, j0+8]
-    R id[R1Y][R1X];
-    R b[R1Y][R1X];
+    R x[FY][WX];             // rows j in [j0-2, j0+SY+1]
+    R cx[R1Y][WX];           // rows j in [j0-1, j0+SY]
+    R cy[R1Y + 1][WX];       // rows j in [j0-2, j0+SY]
+    R cz[R1Y][WX];
+    R id[R1Y][WX];
+    R b[R1Y][WX];
 };
+constexpr int SLOT_ROWS = FY + R1Y + (R1Y + 1) + 3 * R1Y;   // 63 staged rows per plane
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool ok) {
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool ok) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
-                 "r"(ok ? 4 : 0));
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool ok) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem),
-                 "r"(ok ? 8 : 0));
-}
-template <typename R>
-__device__ __forceinline__ void cp_async_el(R* smem, const R* gmem, bool ok) {
-    if (sizeof(R) == 4) cp_async4(smem, gmem, ok);
-    else cp_async8(smem, gmem, ok);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(ok ? 16 : 0));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // ZERO: xin is zero (first pre-smoothing sweep).  xc != null: prolongation
-// x += x_{l+1}(parent) fused into the loads.  dot != null: accumulate b.xout.
+// x += x_{l+1}(parent) fused into the staged x.  dot != null: accumulate b.xout.
+// Every staged row is a 16-byte aligned window of WX elements starting at
+// i = i0 - 4 (XOFF and the pitches make at(i0-4, j, k) a multiple of 4
+// elements); each thread owns fixed 16-byte chunks of the slot, so its copy
+// addresses are precomputed once and advanced by one plane stride per plane.
 template <typename R, bool ZERO>
 __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __restrict__ cx,
                                                          const R* __restrict__ cy,
@@ -231,59 +227,92 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
                                                          double* dot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SweepSlot<R>* slots = reinterpret_cast<SweepSlot<R>*>(smem_raw);
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * SX + tx;
     constexpr int NT = SX * SY;
+    constexpr int EPC = 16 / sizeof(R);               // elements per 16-byte chunk
+    constexpr int CPR = WX / EPC;                     // chunks per staged row
+    constexpr int NCH = SLOT_ROWS * CPR;              // chunks per plane
+    constexpr int MAXC = (NCH + NT - 1) / NT;         // chunks per thread
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * SX + tx;
     const int i0 = 1 + blockIdx.x * SX, j0 = 1 + blockIdx.y * SY;
     const int k0 = 1 + blockIdx.z * SZC;
     const int k1 = min(g.nz, k0 + SZC - 1);
     R dacc = 0;
+
+    // this thread's chunks: source array, row offset (plane 0), smem offset, row j
+    const R* csrc[MAXC];
+    long long coff[MAXC];
+    int csm[MAXC], cj[MAXC], ci[MAXC];
+    bool cx_ok[MAXC], cis_x[MAXC];
+#pragma unroll
+    for (int s = 0; s < MAXC; ++s) {
+        const int q = tid + s * NT;
+        csrc[s] = nullptr;
+        coff[s] = 0;
+        csm[s] = 0;
+        cj[s] = -1;
+        ci[s] = 0;
+        cx_ok[s] = false;
+        cis_x[s] = false;
+        if (q >= NCH) continue;
+        const int row = q / CPR, ch = q - row * CPR;
+        int j, srow;
+        const R* src;
+        if (row < FY) { src = xin; j = j0 - 2 + row; srow = row; cis_x[s] = true; }
+        else if (row < FY + R1Y) { src = cx; j = j0 - 1 + (row - FY); srow = row; }
+        else if (row < FY + 2 * R1Y + 1) { src = cy; j = j0 - 2 + (row - FY - R1Y); srow = row; }
+        else {
+            const int r3 = row - (FY + 2 * R1Y + 1);
+            const int which = r3 / R1Y;
+            src = which == 0 ? cz : (which == 1 ? idiag : b);
+            j = j0 - 1 + (r3 - which * R1Y);
+            srow = row;
+        }
+        const int e0 = i0 - 4 + ch * EPC;
+        csrc[s] = src;
+        cj[s] = j;
+        ci[s] = e0;
+        cx_ok[s] = j >= 0 && j <= g.ny + 1 && e0 <= g.nx + 1;
+        coff[s] = XOFF + (long long)j * g.P + e0;
+        csm[s] = srow * WX + ch * EPC;
+    }
+    auto slot_base = [&](int k) -> R* {
+        return reinterpret_cast<R*>(&slots[(k + 2 * NSLOT) % NSLOT]);
+    };
     auto slot = [&](int k) -> SweepSlot<R>& { return slots[(k + 2 * NSLOT) % NSLOT]; };
-    // inside the allocated halo box (values there are the array's: 0 on halos)
-    auto inbox = [&](int i, int j, int k) {
-        return i >= 0 && i <= g.nx + 1 && j >= 0 && j <= g.ny + 1 && k >= 0 && k <= g.nz + 1;
-    };
-    auto interior = [&](int i, int j, int k) {
-        return i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz;
-    };
     auto issue = [&](int k) {
-        SweepSlot<R>& S = slot(k);
-        for (int q = tid; q < FX * FY; q += NT) {
-            const int fj = q / FX, fi = q - fj * FX, i = i0 - 2 + fi, j = j0 - 2 + fj;
-            if (ZERO) {
-                S.x[fj][fi] = 0;   // old x is zero; halo / ring entries must read as 0
-            } else {
-                const bool ok = inbox(i, j, k);
-                cp_async_el(&S.x[fj][fi], ok ? xin + g.at(i, j, k) : xin, ok);
+        R* base = slot_base(k);
+        const bool kok = k >= 0 && k <= g.nz + 1;
+#pragma unroll
+        for (int s = 0; s < MAXC; ++s) {
+            if (!csrc[s] && !(ZERO && cis_x[s])) continue;
+            if (ZERO && cis_x[s]) {
+                if (cj[s] >= 0 || true) {
+                    R* d = base + csm[s];
+#pragma unroll
+                    for (int e = 0; e < EPC; ++e) d[e] = 0;
+                }
+                continue;
             }
-        }
-        for (int q = tid; q < R1Y * (R1X + 1); q += NT) {
-            const int c = q / (R1X + 1), a = q - c * (R1X + 1), i = i0 - 2 + a, j = j0 - 1 + c;
-            const bool ok = inbox(i, j, k);
-            cp_async_el(&S.cx[c][a], ok ? cx + g.at(i, j, k) : cx, ok);
-        }
-        for (int q = tid; q < (R1Y + 1) * R1X; q += NT) {
-            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 2 + c;
-            const bool ok = inbox(i, j, k);
-            cp_async_el(&S.cy[c][a], ok ? cy + g.at(i, j, k) : cy, ok);
-        }
-        for (int q = tid; q < R1Y * R1X; q += NT) {
-            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 1 + c;
-            const bool ok = inbox(i, j, k);
-            const long long n = ok ? g.at(i, j, k) : 0;
-            cp_async_el(&S.cz[c][a], cz + n, ok);
-            cp_async_el(&S.id[c][a], idiag + n, ok);
-            cp_async_el(&S.b[c][a], b + n, ok);
+            const bool ok = kok && cx_ok[s];
+            const R* src = ok ? csrc[s] + coff[s] + (long long)k * g.S : csrc[s];
+            cp_async16(base + csm[s], src, ok);
         }
         cp_async_commit();
     };
-    // after the slot of plane k has landed: add the coarse correction to the
-    // x values this thread copied (its own cp.async results are visible to it)
+    // after plane k has landed: add the coarse correction to this thread's x chunks
     auto correct = [&](int k) {
-        if (ZERO || !xc) return;
-        SweepSlot<R>& S = slot(k);
-        for (int q = tid; q < FX * FY; q += NT) {
-            const int fj = q / FX, fi = q - fj * FX, i = i0 - 2 + fi, j = j0 - 2 + fj;
-            if (interior(i, j, k)) S.x[fj][fi] += xc[gc.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+        if (ZERO || !xc || k < 1 || k > g.nz) return;
+        R* base = slot_base(k);
+        const int K = (k + 1) >> 1;
+#pragma unroll
+        for (int s = 0; s < MAXC; ++s) {
+            if (!cis_x[s] || cj[s] < 1 || cj[s] > g.ny) continue;
+            const int J = (cj[s] + 1) >> 1;
+#pragma unroll
+            for (int e = 0; e < EPC; ++e) {
+                const int i = ci[s] + e;
+                if (i >= 1 && i <= g.nx) base[csm[s] + e] += xc[gc.at((i + 1) >> 1, J, K)];
+            }
         }
     };
     auto first_colour = [&](int k) {
@@ -294,30 +323,31 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         for (int q = tid; q < R1Y * R1X; q += NT) {
             const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 1 + c;
             if (i < 1 || i > g.nx || j < 1 || j > g.ny || ((i + j + k) & 1) != c0) continue;
-            R s = S.b[c][a];
+            const int w = a + 3;
+            R s = S.b[c][w];
             if (!ZERO)
-                s += S.cx[c][a + 1] * S.x[c + 1][a + 2] + S.cx[c][a] * S.x[c + 1][a] +
-                     S.cy[c + 1][a] * S.x[c + 2][a + 1] + S.cy[c][a] * S.x[c][a + 1] +
-                     S.cz[c][a] * Sp.x[c + 1][a + 1] + Sm.cz[c][a] * Sm.x[c + 1][a + 1];
-            S.x[c + 1][a + 1] = S.id[c][a] * s;
+                s += S.cx[c][w] * S.x[c + 1][w + 1] + S.cx[c][w - 1] * S.x[c + 1][w - 1] +
+                     S.cy[c + 1][w] * S.x[c + 2][w] + S.cy[c][w] * S.x[c][w] +
+                     S.cz[c][w] * Sp.x[c + 1][w] + Sm.cz[c][w] * Sm.x[c + 1][w];
+            S.x[c + 1][w] = S.id[c][w] * s;
         }
     };
     auto second_colour = [&](int k) {
         const SweepSlot<R>& S = slot(k);
         const SweepSlot<R>& Sm = slot(k - 1);
         const SweepSlot<R>& Sp = slot(k + 1);
-        const int a = tx + 1, c = ty + 1, i = i0 + tx, j = j0 + ty;
+        const int c = ty + 1, w = tx + 4, i = i0 + tx, j = j0 + ty;
         if (i <= g.nx && j <= g.ny) {
-            R v = S.x[c + 1][a + 1];
+            R v = S.x[c + 1][w];
             if (((i + j + k) & 1) != c0) {
-                const R s = S.b[c][a] + S.cx[c][a + 1] * S.x[c + 1][a + 2] +
-                            S.cx[c][a] * S.x[c + 1][a] + S.cy[c + 1][a] * S.x[c + 2][a + 1] +
-                            S.cy[c][a] * S.x[c][a + 1] + S.cz[c][a] * Sp.x[c + 1][a + 1] +
-                            Sm.cz[c][a] * Sm.x[c + 1][a + 1];
-                v = S.id[c][a] * s;
+                const R s = S.b[c][w] + S.cx[c][w] * S.x[c + 1][w + 1] +
+                            S.cx[c][w - 1] * S.x[c + 1][w - 1] + S.cy[c + 1][w] * S.x[c + 2][w] +
+                            S.cy[c][w] * S.x[c][w] + S.cz[c][w] * Sp.x[c + 1][w] +
+                            Sm.cz[c][w] * Sm.x[c + 1][w];
+                v = S.id[c][w] * s;
             }
             xout[g.at(i, j, k)] = v;
-            if (dot) dacc += S.b[c][a] * v;
+            if (dot) dacc += S.b[c][w] * v;
         }
     };
 
@@ -329,8 +359,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     __syncthreads();
     first_colour(k0);
     for (int k = k0; k <= k1; ++k) {
-        __syncthreads();                      // the slot of plane k+4 held plane k-2
-        issue(k + 4);
+        issue(k + 4);                         // the slot of plane k-3, idle since k-2
         cp_async_wait<2>();                   // plane k+2 landed
         correct(k + 2);
         __syncthreads();
@@ -515,7 +544,7 @@ __global__ void __launch_bounds__(RB) k_apply_p(Grid g, const R* __restrict__ cx
     const R beta = sbeta;
     const long long sy = g.P, sz = g.S;
     R d = 0;
-    ROW_LOOP(g) {
+    ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         auto P = [&](long long m) { return first ? z[m] : z[m] + beta * pold[m]; };
         const R pc = P(n);
@@ -541,7 +570,7 @@ __global__ void __launch_bounds__(RB) k_update_xr(Grid g, R* __restrict__ x, R* 
     __syncthreads();
     const R alpha = salpha;
     R d = 0;
-    ROW_LOOP(g) {
+    ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         x[n] = first ? alpha * p[n] : x[n] + alpha * p[n];
         const R rn = r[n] - alpha * q[n];
@@ -555,7 +584,7 @@ template <typename R>
 __global__ void __launch_bounds__(RB) k_dot(Grid g, const R* __restrict__ a,
                                             const R* __restrict__ b, double* acc) {
     R d = 0;
-    ROW_LOOP(g) {
+    ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         d += a[n] * b[n];
     }
