@@ -315,40 +315,50 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             }
         }
     };
-    auto first_colour = [&](int k) {
-        if (k < 1 || k > g.nz) return;
-        SweepSlot<R>& S = slot(k);
-        const SweepSlot<R>& Sm = slot(k - 1);
-        const SweepSlot<R>& Sp = slot(k + 1);
-        for (int q = tid; q < R1Y * R1X; q += NT) {
-            const int c = q / R1X, a = q - c * R1X, i = i0 - 1 + a, j = j0 - 1 + c;
-            if (i < 1 || i > g.nx || j < 1 || j > g.ny || ((i + j + k) & 1) != c0) continue;
-            const int w = a + 3;
-            R s = S.b[c][w];
-            if (!ZERO)
-                s += S.cx[c][w] * S.x[c + 1][w + 1] + S.cx[c][w - 1] * S.x[c + 1][w - 1] +
-                     S.cy[c + 1][w] * S.x[c + 2][w] + S.cy[c][w] * S.x[c][w] +
-                     S.cz[c][w] * Sp.x[c + 1][w] + Sm.cz[c][w] * Sm.x[c + 1][w];
-            S.x[c + 1][w] = S.id[c][w] * s;
-        }
+    // Updated value of the cell at slot column w, slot row c (R1 row) of plane k.
+    auto relax = [&](const SweepSlot<R>& S, const SweepSlot<R>& Sm, const SweepSlot<R>& Sp, int c,
+                     int w) -> R {
+        R s = S.b[c][w];
+        if (!ZERO)
+            s += S.cx[c][w] * S.x[c + 1][w + 1] + S.cx[c][w - 1] * S.x[c + 1][w - 1] +
+                 S.cy[c + 1][w] * S.x[c + 2][w] + S.cy[c][w] * S.x[c][w] +
+                 S.cz[c][w] * Sp.x[c + 1][w] + Sm.cz[c][w] * Sm.x[c + 1][w];
+        return S.id[c][w] * s;
     };
+    // First colour of plane k on the tile + ring: thread t < 17*R1Y takes the
+    // m-th cell of that colour in R1 row c (every other cell of the row).
+    auto first_colour = [&](int k) {
+        constexpr int PER_ROW = R1X / 2;
+        if (k < 1 || k > g.nz || tid >= PER_ROW * R1Y) return;
+        const int c = tid / PER_ROW, m = tid - c * PER_ROW;
+        const int j = j0 - 1 + c;
+        const int a = 2 * m + ((c0 - (i0 - 1) - j - k) & 1);
+        const int i = i0 - 1 + a;
+        if (i < 1 || i > g.nx || j < 1 || j > g.ny) return;
+        SweepSlot<R>& S = slot(k);
+        S.x[c + 1][a + 3] = relax(S, slot(k - 1), slot(k + 1), c, a + 3);
+    };
+    // Second colour of plane k on the tile: thread t < 16*SY takes the m-th
+    // cell of that colour in tile row r; the values stay in shared memory.
     auto second_colour = [&](int k) {
+        constexpr int PER_ROW = SX / 2;
+        if (tid >= PER_ROW * SY) return;
+        const int r = tid / PER_ROW, m = tid - r * PER_ROW;
+        const int j = j0 + r;
+        const int i = i0 + 2 * m + ((c0 + 1 - i0 - j - k) & 1);
+        if (i > g.nx || j > g.ny) return;
+        SweepSlot<R>& S = slot(k);
+        const int w = i - i0 + 4;
+        S.x[r + 2][w] = relax(S, slot(k - 1), slot(k + 1), r + 1, w);
+    };
+    // Coalesced store of the finished tile of plane k (both colours).
+    auto write_out = [&](int k) {
+        const int i = i0 + tx, j = j0 + ty;
+        if (i > g.nx || j > g.ny) return;
         const SweepSlot<R>& S = slot(k);
-        const SweepSlot<R>& Sm = slot(k - 1);
-        const SweepSlot<R>& Sp = slot(k + 1);
-        const int c = ty + 1, w = tx + 4, i = i0 + tx, j = j0 + ty;
-        if (i <= g.nx && j <= g.ny) {
-            R v = S.x[c + 1][w];
-            if (((i + j + k) & 1) != c0) {
-                const R s = S.b[c][w] + S.cx[c][w] * S.x[c + 1][w + 1] +
-                            S.cx[c][w - 1] * S.x[c + 1][w - 1] + S.cy[c + 1][w] * S.x[c + 2][w] +
-                            S.cy[c][w] * S.x[c][w] + S.cz[c][w] * Sp.x[c + 1][w] +
-                            Sm.cz[c][w] * Sm.x[c + 1][w];
-                v = S.id[c][w] * s;
-            }
-            xout[g.at(i, j, k)] = v;
-            if (dot) dacc += S.b[c][w] * v;
-        }
+        const R v = S.x[ty + 2][tx + 4];
+        xout[g.at(i, j, k)] = v;
+        if (dot) dacc += S.b[ty + 1][tx + 4] * v;
     };
 
     for (int k = k0 - 2; k <= k0 + 3; ++k) issue(k);
@@ -363,10 +373,13 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         cp_async_wait<2>();                   // plane k+2 landed
         correct(k + 2);
         __syncthreads();
+        if (k > k0) write_out(k - 1);
         first_colour(k + 1);
         __syncthreads();
         second_colour(k);
     }
+    __syncthreads();
+    write_out(k1);
     cp_async_wait<0>();
     if (dot) block_add(dacc, dot);
 }
@@ -544,7 +557,7 @@ __global__ void __launch_bounds__(RB) k_apply_p(Grid g, const R* __restrict__ cx
     const R beta = sbeta;
     const long long sy = g.P, sz = g.S;
     R d = 0;
-    ROW_LOOP_U4(g) {
+    ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         auto P = [&](long long m) { return first ? z[m] : z[m] + beta * pold[m]; };
         const R pc = P(n);
@@ -668,7 +681,7 @@ static void rbgs_grid(const Grid& g, dim3& gr, dim3& b) {
 }
 
 static long long ncells(const Grid& g) { return (long long)g.nx * g.ny * g.nz; }
-constexpr long long BIG_CELLS = 1LL << 20;   // default: levels swept by the pipelined kernel
+constexpr long long BIG_CELLS = 1LL << 23;   // default: levels swept by the pipelined kernel
 
 // One V-cycle z = M r (level 0 aliases b = r, x = z); rz != null accumulates
 // r.z (in the last level-0 sweep when that level is a big one, else by a dot).

@@ -233,14 +233,15 @@ def test_not_converged_reported():
 
 
 def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
-    """The one-pass pipelined red-black sweep (levels of >= 2^20 cells) gives
-    the same V-cycle as the two-kernel half-sweeps: same PCG iterations and
-    the same pressure to FP32 rounding."""
+    """The one-pass pipelined red-black sweep gives the same V-cycle as the
+    two-kernel half-sweeps: same PCG iterations and the same pressure to FP32
+    rounding.  The threshold 1 forces the pipelined kernel on every level
+    above the single-block bottom levels (128x128x64 down to 32x32x16)."""
     _, Simulation = _sim_mod()
     case = _case((128, 128, 64), seed=21, log_var=2.0, corr_len=6.0)
     p = case.params
     out = {}
-    for name, thr in (("pipelined", 0), ("half", 1 << 40)):
+    for name, thr in (("pipelined", 1), ("half", 1 << 40)):
         with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="mixed",
                         rtol=1e-10, sweep_min_cells=thr) as sim:
             sim.calcPermeability()
