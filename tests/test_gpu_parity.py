@@ -242,11 +242,11 @@ def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
     p = case.params
     out = {}
     for name, thr in (("pipelined", 1), ("half", 1 << 40)):
-        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="mixed",
-                        rtol=1e-10, sweep_min_cells=thr) as sim:
+        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="fp64",
+                        rtol=1e-12, sweep_min_cells=thr) as sim:
             sim.calcPermeability()
             st = sim.solvePressure()
-            assert st.converged and st.relres <= 1e-10
+            assert st.converged and st.relres <= 1e-12
             out[name] = (st.inner_iterations, sim.download("pressure"))
     assert abs(out["pipelined"][0] - out["half"][0]) <= 1
     assert rel_l2(out["pipelined"][1], out["half"][1]) < 1e-9
