@@ -315,11 +315,13 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             }
         }
     };
-    // Updated value of the cell at slot column w, slot row c (R1 row) of plane k.
+    // Updated value of the cell at slot column w, slot row c (R1 row) of plane
+    // k; neighbours = false when they are all known to be zero (first colour
+    // of the zero-guess sweep).
     auto relax = [&](const SweepSlot<R>& S, const SweepSlot<R>& Sm, const SweepSlot<R>& Sp, int c,
-                     int w) -> R {
+                     int w, bool neighbours) -> R {
         R s = S.b[c][w];
-        if (!ZERO)
+        if (neighbours)
             s += S.cx[c][w] * S.x[c + 1][w + 1] + S.cx[c][w - 1] * S.x[c + 1][w - 1] +
                  S.cy[c + 1][w] * S.x[c + 2][w] + S.cy[c][w] * S.x[c][w] +
                  S.cz[c][w] * Sp.x[c + 1][w] + Sm.cz[c][w] * Sm.x[c + 1][w];
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         const int i = i0 - 1 + a;
         if (i < 1 || i > g.nx || j < 1 || j > g.ny) return;
         SweepSlot<R>& S = slot(k);
-        S.x[c + 1][a + 3] = relax(S, slot(k - 1), slot(k + 1), c, a + 3);
+        S.x[c + 1][a + 3] = relax(S, slot(k - 1), slot(k + 1), c, a + 3, !ZERO);
     };
     // Second colour of plane k on the tile: thread t < 16*SY takes the m-th
     // cell of that colour in tile row r; the values stay in shared memory.
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         if (i > g.nx || j > g.ny) return;
         SweepSlot<R>& S = slot(k);
         const int w = i - i0 + 4;
-        S.x[r + 2][w] = relax(S, slot(k - 1), slot(k + 1), r + 1, w);
+        S.x[r + 2][w] = relax(S, slot(k - 1), slot(k + 1), r + 1, w, true);
     };
     // Coalesced store of the finished tile of plane k (both colours).
     auto write_out = [&](int k) {
