@@ -39,6 +39,7 @@ extern "C" {
 #define WPF_ERR_TIMEOUT        5   /* a bounded device wait expired                */
 #define WPF_ERR_NOMEM          6   /* device allocation failed                     */
 #define WPF_ERR_SINGULAR       7   /* no Dirichlet cell: the Darcy system is singular */
+#define WPF_ERR_TOO_LARGE      8   /* grid beyond the fixed scratch of wpf_reduce_noalloc */
 
 /* ---- solver modes ------------------------------------------------------ */
 #define WPF_SOLVER_FP64   0   /* plain FP64 MG-PCG (the drop-in form)                     */
@@ -158,6 +159,27 @@ int wpf_run(wpf_handle* h, int32_t itime0, int32_t nsteps, double* dtime_inout,
 
 /* Diagnostics of showProgress / getPressure on the device.                  */
 int wpf_reduce(wpf_handle* h, wpf_diag* d);
+
+/* Allocation-free diagnostics.  No counterpart in the reference: an addition
+ * for callers that cannot call cudaMalloc -- code running while a CUDA graph
+ * is captured (allocation cannot be captured), code whose device memory
+ * belongs to another runtime's pool allocator, and latency-critical code that
+ * cannot afford cudaMalloc's implicit device synchronisation.  It computes
+ * pv, vcal, rwhmax and the phase / concentration max and min of wpf_diag
+ * (pressure_ref and inlet_flux are returned as 0) from device arrays the
+ * caller already holds: d_phase and d_concent are G-sized float64 arrays in
+ * the reference layout (Fortran order with the one-cell halo).  Its scratch
+ * is one fixed file-scope device array of WPF_NOALLOC_MAX_PLANES records
+ * (about 360 KB), reserved on every GPU that loads the library until the
+ * process exits; grids with nz + 2 > WPF_NOALLOC_MAX_PLANES are rejected with
+ * WPF_ERR_TOO_LARGE.  The first call on a device looks up the scratch's
+ * device address (once per device), so make that first call before any
+ * stream capture.  Work is ordered on `stream` (a cudaStream_t; NULL = the
+ * default stream) and the call returns after it finishes.  Every call shares
+ * the one scratch array, so calls that overlap on the GPU race.             */
+#define WPF_NOALLOC_MAX_PLANES 4096
+int wpf_reduce_noalloc(const wpf_params* p, const double* d_phase, const double* d_concent,
+                       wpf_diag* out, void* stream);
 
 /* Last taumin on the device (the lagged input of the dt law).               */
 int wpf_get_taumin(const wpf_handle* h, double* taumin);

@@ -19,6 +19,8 @@ WPF_ERR_NONFINITE = 4
 WPF_ERR_TIMEOUT = 5
 WPF_ERR_NOMEM = 6
 WPF_ERR_SINGULAR = 7
+WPF_ERR_TOO_LARGE = 8
+NOALLOC_MAX_PLANES = 4096
 
 SOLVER_FP64 = 0
 SOLVER_MIXED = 1
@@ -96,6 +98,8 @@ SIGNATURES = {
     "wpf_step": (C.c_int, [H, C.c_int32, DP, C.POINTER(StepStats)]),
     "wpf_run": (C.c_int, [H, C.c_int32, C.c_int32, DP, C.POINTER(StepStats)]),
     "wpf_reduce": (C.c_int, [H, C.POINTER(Diag)]),
+    "wpf_reduce_noalloc": (C.c_int, [C.POINTER(Params), C.c_void_p, C.c_void_p,
+                                     C.POINTER(Diag), C.c_void_p]),
     "wpf_get_taumin": (C.c_int, [H, DP]),
     "wpf_get_stream": (C.c_int, [H, C.POINTER(C.c_void_p)]),
     "wpf_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),

@@ -127,6 +127,8 @@ const char* wpf_strerror(int s) {
         case WPF_ERR_TIMEOUT: return "bounded device wait expired";
         case WPF_ERR_NOMEM: return "device allocation failed";
         case WPF_ERR_SINGULAR: return "no Dirichlet cell: the Darcy system is singular";
+        case WPF_ERR_TOO_LARGE:
+            return "grid exceeds the fixed scratch of wpf_reduce_noalloc (nz + 2 > 4096 planes)";
         default: return "unknown status";
     }
 }
