@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--w-from", type=int, default=0,
+                    help="first multigrid level cycled twice (0 = library default)")
     ap.add_argument("--breakdown", action="store_true",
                     help="time every kernel class (diagnostic run; adds event overhead)")
     return ap.parse_args()
@@ -174,7 +176,7 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     case = make_workload(args, rank)
     sim = Simulation(case.params, case.permeab_rock, case.phase, case.concent,
-                     solver=args.solver, rtol=args.rtol)
+                     solver=args.solver, rtol=args.rtol, w_from_level=args.w_from)
     L = sim.L
     for _ in range(args.warmup):
         sim.step()

@@ -80,7 +80,10 @@ typedef struct wpf_solver_opts {
     double rtol;               /* ||b - A p|| <= rtol * ||b|| (true FP64 residual)      */
     double inner_rtol;         /* inner PCG reduction per pass in MIXED mode (1e-4)    */
     int64_t sweep_min_cells;   /* levels with at least this many cells use the pipelined
-                                  one-pass sweep kernel (0 = default 2^20)              */
+                                  one-pass sweep kernel (0 = default 2^23)              */
+    int32_t w_from_level;      /* levels >= this (and below the pipelined ones) recurse
+                                  twice: a W-cycle (0 = default 2; large = V-cycle)     */
+    int32_t pad;
 } wpf_solver_opts;
 
 /* Per-step / per-solve statistics. */

@@ -50,7 +50,7 @@ class Well(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_outer", C.c_int32), ("max_inner", C.c_int32),
                 ("smooth_sweeps", C.c_int32), ("rtol", C.c_double), ("inner_rtol", C.c_double),
-                ("sweep_min_cells", C.c_int64)]
+                ("sweep_min_cells", C.c_int64), ("w_from_level", C.c_int32), ("pad", C.c_int32)]
 
 
 class StepStats(C.Structure):

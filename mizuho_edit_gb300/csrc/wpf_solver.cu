@@ -456,10 +456,14 @@ __global__ void k_resid_restrict(Grid f, Grid c, const R* __restrict__ cx, const
     bc[c.at(I, J, K)] = s;
 }
 
-// Levels with at most BOTTOM_CELLS cells: the whole sub-V-cycle (same
-// smoother, restriction and prolongation as above) in one block.
-constexpr int BOTTOM_CELLS = 4096;
+// The coarsest levels (at most bottom_cells<R>() cells on the first of them)
+// run their whole sub-cycle in one 1024-thread block, with every array of
+// those levels copied into shared memory in a compact halo-free layout
+// (neighbours outside the grid read as zero; their couplings are zero).
 constexpr int BOTTOM_THREADS = 1024;
+constexpr size_t BOTTOM_SMEM_MAX = 200 * 1024;   // bound on the staged bottom levels
+template <typename R>
+constexpr long long bottom_cells() { return sizeof(R) == 4 ? 4096 : 512; }
 
 template <typename R>
 struct BottomArgs {
@@ -468,75 +472,119 @@ struct BottomArgs {
 };
 
 template <typename R>
-__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(BottomArgs<R> A) {
-    const int T = blockDim.x;
-    auto colour_sweep = [&](const Level<R>& L, int color) {
-        const Grid& g = L.g;
-        const int nc = g.nx * g.ny * g.nz;
-        for (int q = threadIdx.x; q < nc; q += T) {
-            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
-            if (((i + j + k) & 1) != color) continue;
-            const long long n = g.at(i, j, k);
-            L.x[n] = L.idiag[n] * (L.b[n] + offsum(L.cx, L.cy, L.cz, L.x, n, g.P, g.S));
-        }
-        __syncthreads();
-    };
-    auto zero_x = [&](const Level<R>& L) {
-        const Grid& g = L.g;
-        const int nc = g.nx * g.ny * g.nz;
-        for (int q = threadIdx.x; q < nc; q += T) {
-            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
-            L.x[g.at(i, j, k)] = 0;
-        }
-        __syncthreads();
-    };
-    const int last = A.nlev - 1;
-    for (int l = A.l0; l <= last; ++l) {
-        const Level<R>& L = A.lv[l];
-        zero_x(L);
-        if (l == last) {
-            for (int s = 0; s < 16; ++s) { colour_sweep(L, 0); colour_sweep(L, 1); }
-            break;
-        }
-        for (int s = 0; s < A.nu; ++s) { colour_sweep(L, 0); colour_sweep(L, 1); }
-        const Level<R>& C = A.lv[l + 1];
-        const Grid& f = L.g;
-        const Grid& c = C.g;
-        const int ncc = c.nx * c.ny * c.nz;
-        for (int q = threadIdx.x; q < ncc; q += T) {
-            const int I = 1 + q % c.nx, J = 1 + (q / c.nx) % c.ny, K = 1 + q / (c.nx * c.ny);
-            R s = 0;
-            for (int dk = 0; dk < 2; ++dk) {
-                const int k = 2 * K - 1 + dk;
-                if (k > f.nz) break;
-                for (int dj = 0; dj < 2; ++dj) {
-                    const int j = 2 * J - 1 + dj;
-                    if (j > f.ny) break;
-                    for (int di = 0; di < 2; ++di) {
-                        const int i = 2 * I - 1 + di;
-                        if (i > f.nx) break;
-                        const long long n = f.at(i, j, k);
-                        s += L.b[n] - (L.diag[n] * L.x[n] - offsum(L.cx, L.cy, L.cz, L.x, n, f.P, f.S));
-                    }
+struct BLevel {
+    int nx, ny, nz, n;
+    R *cx, *cy, *cz, *d, *id, *x, *b;
+};
+
+template <typename R>
+__device__ __forceinline__ R b_offsum(const BLevel<R>& L, int c, int i, int j, int k) {
+    const int sy = L.nx, sz = L.nx * L.ny;
+    R s = 0;
+    if (i + 1 < L.nx) s += L.cx[c] * L.x[c + 1];
+    if (i > 0) s += L.cx[c - 1] * L.x[c - 1];
+    if (j + 1 < L.ny) s += L.cy[c] * L.x[c + sy];
+    if (j > 0) s += L.cy[c - sy] * L.x[c - sy];
+    if (k + 1 < L.nz) s += L.cz[c] * L.x[c + sz];
+    if (k > 0) s += L.cz[c - sz] * L.x[c - sz];
+    return s;
+}
+
+// colour of a 0-based cell in the 1-based convention of the other kernels
+__device__ __forceinline__ int b_colour(int i, int j, int k) { return (i + j + k + 1) & 1; }
+
+template <typename R>
+__device__ void b_sweep(const BLevel<R>& L, int color) {
+    for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
+        const int i = c % L.nx, r = c / L.nx, j = r % L.ny, k = r / L.ny;
+        if (b_colour(i, j, k) != color) continue;
+        L.x[c] = L.id[c] * (L.b[c] + b_offsum(L, c, i, j, k));
+    }
+    __syncthreads();
+}
+
+template <typename R>
+__device__ void b_cycle(const BLevel<R>* lv, int l, int last, int nu) {
+    const BLevel<R>& L = lv[l];
+    for (int c = threadIdx.x; c < L.n; c += blockDim.x) L.x[c] = 0;
+    __syncthreads();
+    if (l == last) {
+        for (int s = 0; s < 8; ++s) { b_sweep(L, 0); b_sweep(L, 1); }
+        return;
+    }
+    for (int s = 0; s < nu; ++s) { b_sweep(L, 0); b_sweep(L, 1); }
+    const BLevel<R>& C = lv[l + 1];
+    for (int q = threadIdx.x; q < C.n; q += blockDim.x) {
+        const int I = q % C.nx, rr = q / C.nx, J = rr % C.ny, K = rr / C.ny;
+        R s = 0;
+        for (int dk = 0; dk < 2; ++dk) {
+            const int k = 2 * K + dk;
+            if (k >= L.nz) break;
+            for (int dj = 0; dj < 2; ++dj) {
+                const int j = 2 * J + dj;
+                if (j >= L.ny) break;
+                for (int di = 0; di < 2; ++di) {
+                    const int i = 2 * I + di;
+                    if (i >= L.nx) break;
+                    const int c = i + L.nx * (j + L.ny * k);
+                    s += L.b[c] - (L.d[c] * L.x[c] - b_offsum(L, c, i, j, k));
                 }
             }
-            C.b[c.at(I, J, K)] = s;
         }
-        __syncthreads();
+        C.b[q] = s;
     }
-    for (int l = last - 1; l >= A.l0; --l) {
-        const Level<R>& L = A.lv[l];
-        const Level<R>& C = A.lv[l + 1];
-        const Grid& g = L.g;
-        const int nc = g.nx * g.ny * g.nz;
-        for (int q = threadIdx.x; q < nc; q += T) {
-            const int i = 1 + q % g.nx, j = 1 + (q / g.nx) % g.ny, k = 1 + q / (g.nx * g.ny);
-            const long long n = g.at(i, j, k);
-            if (L.idiag[n] != (R)0) L.x[n] += C.x[C.g.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+    __syncthreads();
+    b_cycle(lv, l + 1, last, nu);
+    for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
+        const int i = c % L.nx, r = c / L.nx, j = r % L.ny, k = r / L.ny;
+        if (L.id[c] != (R)0) L.x[c] += C.x[(i >> 1) + C.nx * ((j >> 1) + C.ny * (k >> 1))];
+    }
+    __syncthreads();
+    for (int s = 0; s < nu; ++s) { b_sweep(L, 1); b_sweep(L, 0); }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(BottomArgs<R> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sp = reinterpret_cast<R*>(smem_raw);
+    __shared__ BLevel<R> lv[MAX_LEVELS];
+    if (threadIdx.x == 0) {
+        R* p = sp;
+        for (int l = A.l0; l < A.nlev; ++l) {
+            const Grid& g = A.lv[l].g;
+            BLevel<R>& B = lv[l];
+            B.nx = g.nx; B.ny = g.ny; B.nz = g.nz; B.n = g.nx * g.ny * g.nz;
+            R** arrs[7] = {&B.cx, &B.cy, &B.cz, &B.d, &B.id, &B.x, &B.b};
+            for (auto a : arrs) { *a = p; p += B.n; }
         }
-        __syncthreads();
-        for (int s = 0; s < A.nu; ++s) { colour_sweep(L, 1); colour_sweep(L, 0); }
     }
+    __syncthreads();
+    for (int l = A.l0; l < A.nlev; ++l) {   // stage the operators and the top right-hand side
+        const Level<R>& G = A.lv[l];
+        const BLevel<R>& B = lv[l];
+        for (int c = threadIdx.x; c < B.n; c += blockDim.x) {
+            const int i = c % B.nx, r = c / B.nx, j = r % B.ny, k = r / B.ny;
+            const long long n = G.g.at(i + 1, j + 1, k + 1);
+            B.cx[c] = G.cx[n]; B.cy[c] = G.cy[n]; B.cz[c] = G.cz[n];
+            B.d[c] = G.diag[n]; B.id[c] = G.idiag[n];
+            if (l == A.l0) B.b[c] = G.b[n];
+        }
+    }
+    __syncthreads();
+    b_cycle(lv, A.l0, A.nlev - 1, A.nu);
+    const Level<R>& G = A.lv[A.l0];
+    const BLevel<R>& B = lv[A.l0];
+    for (int c = threadIdx.x; c < B.n; c += blockDim.x) {
+        const int i = c % B.nx, r = c / B.nx, j = r % B.ny, k = r / B.ny;
+        G.x[G.g.at(i + 1, j + 1, k + 1)] = B.x[c];
+    }
+}
+
+template <typename R>
+static size_t bottom_smem(const Hierarchy<R>& H, int l0) {
+    size_t cells = 0;
+    for (int l = l0; l < H.nlev; ++l) cells += (size_t)H.lv[l].g.nx * H.lv[l].g.ny * H.lv[l].g.nz;
+    return cells * 7 * sizeof(R);
 }
 
 // ---- PCG vector kernels (persistent row loops, one atomic per block) -------
@@ -685,91 +733,105 @@ static void rbgs_grid(const Grid& g, dim3& gr, dim3& b) {
 static long long ncells(const Grid& g) { return (long long)g.nx * g.ny * g.nz; }
 constexpr long long BIG_CELLS = 1LL << 23;   // default: levels swept by the pipelined kernel
 
-// One V-cycle z = M r (level 0 aliases b = r, x = z); rz != null accumulates
-// r.z (in the last level-0 sweep when that level is a big one, else by a dot).
-// Big levels sweep between their two buffers so that the 2*nu sweeps end in
-// the level's output buffer x (the first pre-sweep writes xs, the last
-// post-sweep writes x); mid levels sweep x in place; the levels with at most
-// BOTTOM_CELLS cells run in one k_bottom block.
+// One preconditioner cycle z = M r (level 0 aliases b = r, x = z); rz != null
+// accumulates r.z (in the last level-0 sweep when that level is a big one,
+// else by a dot).  Level l recurses gamma(l) times (gamma = 2 from level
+// opts.w_from_level on: a W-cycle on the mid levels; 1 above: a V-cycle),
+// with symmetric smoothing around each coarse correction, so the cycle stays
+// a symmetric preconditioner.  Big levels sweep between their two buffers so
+// that the 2*nu sweeps end in the level's output buffer x (the first
+// pre-sweep writes xs, the last post-sweep writes x); mid levels sweep x in
+// place; the levels from the first one with at most bottom_cells<R>() cells
+// run in one k_bottom block.
 template <typename R>
-static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu, double* rz) {
+static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, long long big,
+                        int wfrom, double* rz, bool& need_dot) {
     cudaStream_t s = h->stream;
     const dim3 sb(SX, SY);
-    const R* pre_end[MAX_LEVELS];
-    const long long big = h->opts.sweep_min_cells > 0 ? h->opts.sweep_min_cells : BIG_CELLS;
-    int lb = H.nlev - 1;
-    while (lb > 0 && ncells(H.lv[lb - 1].g) <= BOTTOM_CELLS) --lb;
-    for (int l = 0; l < lb; ++l) {
-        Level<R>& L = H.lv[l];
-        const Grid& g = L.g;
-        const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
-        if (ncells(g) >= big) {
-            R* buf[2] = {L.xs, L.x};
-            for (int it = 0; it < nu; ++it) {
-                const R* in = buf[(it + 1) & 1];
-                R* out = buf[it & 1];
-                if (it == 0)
-                    WPF_LAUNCH(h, cls, k_sweep_async<R, true><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                        g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
-                else
-                    WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                        g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
-            }
-            pre_end[l] = buf[(nu - 1) & 1];
-        } else {
-            dim3 b, gr;
-            rbgs_grid<R>(g, gr, b);
-            WPF_LAUNCH(h, cls, k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b));
-            WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
-            for (int it = 1; it < nu; ++it) {
-                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
-                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
-            }
-            pre_end[l] = L.x;
-        }
-        Level<R>& C = H.lv[l + 1];
-        WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
-            g, C.g, L.cx, L.cy, L.cz, L.diag, pre_end[l], L.b, C.b));
-    }
-    {
+    if (l >= lb) {
         BottomArgs<R> A;
         A.l0 = lb;
         A.nlev = H.nlev;
         A.nu = nu;
-        for (int l = 0; l < H.nlev; ++l) A.lv[l] = H.lv[l];
-        WPF_LAUNCH(h, lb == 0 ? KC_SMOOTH0 : KC_MGREST, k_bottom<R><<<1, BOTTOM_THREADS, 0, s>>>(A));
+        for (int q = 0; q < H.nlev; ++q) A.lv[q] = H.lv[q];
+        WPF_LAUNCH(h, lb == 0 ? KC_SMOOTH0 : KC_MGREST,
+                   k_bottom<R><<<1, BOTTOM_THREADS, bottom_smem(H, lb), s>>>(A));
+        return;
     }
-    bool need_dot = rz != nullptr;
-    for (int l = lb - 1; l >= 0; --l) {
-        Level<R>& L = H.lv[l];
-        Level<R>& C = H.lv[l + 1];
-        const Grid& g = L.g;
-        const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
-        if (ncells(g) >= big) {
-            R* buf[2] = {L.xs, L.x};
-            for (int it = 0; it < nu; ++it) {
-                const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
-                const R* in = buf[(w + 1) & 1];
-                R* out = buf[w & 1];
-                const bool last0 = (l == 0 && it == nu - 1 && rz);
-                if (last0) need_dot = false;
+    Level<R>& L = H.lv[l];
+    Level<R>& C = H.lv[l + 1];
+    const Grid& g = L.g;
+    const int cls = l == 0 ? KC_SMOOTH0 : KC_MGREST;
+    const bool is_big = ncells(g) >= big;
+    const int gamma = (l >= wfrom && !is_big) ? 2 : 1;
+    dim3 hb, hg;
+    rbgs_grid<R>(g, hg, hb);
+    auto half_pre = [&](bool zero) {
+        if (zero)
+            WPF_LAUNCH(h, cls, k_rbgs_first<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, L.idiag, L.x, L.b));
+        else
+            WPF_LAUNCH(h, cls, k_rbgs<R><<<hg, hb, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+        WPF_LAUNCH(h, cls, k_rbgs<R><<<hg, hb, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+    };
+    auto half_post = [&]() {
+        WPF_LAUNCH(h, cls, k_rbgs<R><<<hg, hb, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
+        WPF_LAUNCH(h, cls, k_rbgs<R><<<hg, hb, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
+    };
+    if (is_big) {
+        R* buf[2] = {L.xs, L.x};
+        for (int it = 0; it < nu; ++it) {
+            const R* in = buf[(it + 1) & 1];
+            R* out = buf[it & 1];
+            if (it == 0)
+                WPF_LAUNCH(h, cls, k_sweep_async<R, true><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
+                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
+            else
                 WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, it == 0 ? C.x : nullptr, C.g,
-                    last0 ? rz : nullptr));
-            }
-        } else {
-            dim3 b, gr;
-            rbgs_grid<R>(g, gr, b);
-            WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x));
-            for (int it = 0; it < nu; ++it) {
-                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 1));
-                WPF_LAUNCH(h, cls, k_rbgs<R><<<gr, b, 0, s>>>(g, L.cx, L.cy, L.cz, L.idiag, L.x, L.b, 0));
-            }
+                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
+        }
+        const R* pre_end = buf[(nu - 1) & 1];
+        WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
+            g, C.g, L.cx, L.cy, L.cz, L.diag, pre_end, L.b, C.b));
+        cycle_level(h, H, l + 1, lb, nu, big, wfrom, nullptr, need_dot);
+        for (int it = 0; it < nu; ++it) {
+            const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
+            const R* in = buf[(w + 1) & 1];
+            R* out = buf[w & 1];
+            const bool last0 = (l == 0 && it == nu - 1 && rz);
+            if (last0) need_dot = false;
+            WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
+                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, it == 0 ? C.x : nullptr, C.g,
+                last0 ? rz : nullptr));
+        }
+        return;
+    }
+    for (int it = 0; it < nu; ++it) half_pre(it == 0);
+    for (int rep = 0; rep < gamma; ++rep) {
+        WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
+            g, C.g, L.cx, L.cy, L.cz, L.diag, L.x, L.b, C.b));
+        cycle_level(h, H, l + 1, lb, nu, big, wfrom, nullptr, need_dot);
+        WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(g, C.g, L.idiag, L.x, C.x));
+        if (rep + 1 < gamma) {
+            for (int it = 0; it < nu; ++it) half_post();
+            for (int it = 0; it < nu; ++it) half_pre(false);
         }
     }
+    for (int it = 0; it < nu; ++it) half_post();
+}
+
+template <typename R>
+static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu, double* rz) {
+    const long long big = h->opts.sweep_min_cells > 0 ? h->opts.sweep_min_cells : BIG_CELLS;
+    const int wfrom = h->opts.w_from_level > 0 ? h->opts.w_from_level : 2;
+    int lb = H.nlev - 1;
+    while (lb > 0 && ncells(H.lv[lb - 1].g) <= bottom_cells<R>() &&
+           bottom_smem(H, lb - 1) <= BOTTOM_SMEM_MAX)
+        --lb;
+    bool need_dot = rz != nullptr;
+    cycle_level(h, H, 0, lb, nu, big, wfrom, rz, need_dot);
     if (need_dot) {
         const Grid& g = H.lv[0].g;
-        WPF_LAUNCH(h, KC_VEC, k_dot<R><<<row_blocks(h, g), RB, 0, s>>>(g, H.r, H.z, rz));
+        WPF_LAUNCH(h, KC_VEC, k_dot<R><<<row_blocks(h, g), RB, 0, h->stream>>>(g, H.r, H.z, rz));
     }
 }
 
@@ -828,6 +890,8 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
 
 template <typename R>
 static int set_sweep_smem() {
+    WPF_CUDA(cudaFuncSetAttribute(k_bottom<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)BOTTOM_SMEM_MAX));
     WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sweep_smem<R>()));
     WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
