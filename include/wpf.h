@@ -83,8 +83,12 @@ typedef struct wpf_solver_opts {
                                   one-pass sweep kernel (0 = default 2^23)              */
     int32_t w_from_level;      /* levels >= this (and below the pipelined ones) recurse
                                   twice: a W-cycle (0 = default 2; large = V-cycle)     */
-    int32_t pad;
+    int32_t flags;             /* WPF_SOLVER_NO_GRAPHS: launch each preconditioner
+                                  cycle kernel by kernel instead of replaying it as a
+                                  captured CUDA graph (same arithmetic)                 */
 } wpf_solver_opts;
+
+#define WPF_SOLVER_NO_GRAPHS 1
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

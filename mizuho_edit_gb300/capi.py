@@ -24,6 +24,7 @@ NOALLOC_MAX_PLANES = 4096
 
 SOLVER_FP64 = 0
 SOLVER_MIXED = 1
+SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bit
 
 
 class WpfError(RuntimeError):
@@ -50,7 +51,7 @@ class Well(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_outer", C.c_int32), ("max_inner", C.c_int32),
                 ("smooth_sweeps", C.c_int32), ("rtol", C.c_double), ("inner_rtol", C.c_double),
-                ("sweep_min_cells", C.c_int64), ("w_from_level", C.c_int32), ("pad", C.c_int32)]
+                ("sweep_min_cells", C.c_int64), ("w_from_level", C.c_int32), ("flags", C.c_int32)]
 
 
 class StepStats(C.Structure):

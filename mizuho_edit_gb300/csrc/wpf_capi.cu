@@ -29,6 +29,13 @@ int dev_alloc(wpf_handle* h, void** p, size_t bytes) {
 
 int timer_start(wpf_handle* h, int c) {
     if (!(h->timing_mask & (1u << c))) return -1;
+    if (h->cap_ev) {   // capturing a graph: the pair becomes two event record nodes
+        if (*h->cap_ntimers >= h->cap_max) return -1;
+        const int slot = (*h->cap_ntimers)++;
+        h->cap_cls[slot] = c;
+        cudaEventRecordWithFlags(h->cap_ev[2 * slot], h->stream, cudaEventRecordExternal);
+        return slot;
+    }
     if (h->npend >= 256) timer_flush(h);
     if (h->npend >= 256) return -1;
     const int slot = h->npend++;
@@ -38,22 +45,35 @@ int timer_start(wpf_handle* h, int c) {
 }
 
 void timer_stop(wpf_handle* h, int slot) {
-    if (slot >= 0) cudaEventRecord(h->pend_ev[2 * slot + 1], h->stream);
+    if (slot < 0) return;
+    if (h->cap_ev)
+        cudaEventRecordWithFlags(h->cap_ev[2 * slot + 1], h->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(h->pend_ev[2 * slot + 1], h->stream);
+}
+
+static void fold(wpf_handle* h, int cls, cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) {
+        h->kt_ms[cls] += ms;
+        h->kt_count[cls] += 1;
+    } else {
+        cudaGetLastError();
+    }
 }
 
 void timer_flush(wpf_handle* h) {
-    if (!h->npend) return;
-    cudaEventSynchronize(h->pend_ev[2 * h->npend - 1]);
-    for (int s = 0; s < h->npend; ++s) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, h->pend_ev[2 * s], h->pend_ev[2 * s + 1]) == cudaSuccess) {
-            h->kt_ms[h->pend_cls[s]] += ms;
-            h->kt_count[h->pend_cls[s]] += 1;
-        } else {
-            cudaGetLastError();
-        }
+    if (h->npend) {
+        cudaEventSynchronize(h->pend_ev[2 * h->npend - 1]);
+        for (int s = 0; s < h->npend; ++s)
+            fold(h, h->pend_cls[s], h->pend_ev[2 * s], h->pend_ev[2 * s + 1]);
+        h->npend = 0;
     }
-    h->npend = 0;
+    if (h->ngpend) {
+        cudaEventSynchronize(h->gpend_b[h->ngpend - 1]);
+        for (int s = 0; s < h->ngpend; ++s) fold(h, h->gpend_cls[s], h->gpend_a[s], h->gpend_b[s]);
+        h->ngpend = 0;
+    }
 }
 
 int ensure_per_routine_arrays(wpf_handle* h) {
@@ -210,6 +230,8 @@ int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o) {
     if (o->max_outer < 0 || o->max_inner < 1 || !(o->rtol > 0) || o->smooth_sweeps < 0 ||
         o->smooth_sweeps > 16)
         return WPF_ERR_ARG;
+    cudaStreamSynchronize(h->stream);
+    solver_drop_graphs(h);   // the captured cycles bake in nu, the sweep and W-cycle levels
     h->opts = *o;
     if (!(h->opts.inner_rtol > 0 && h->opts.inner_rtol < 1)) h->opts.inner_rtol = 1e-4;
     if (h->opts.smooth_sweeps == 0) h->opts.smooth_sweeps = 2;

@@ -89,6 +89,16 @@ struct Hierarchy {
     // p is double buffered (p, p2) because the operator kernel forms the new
     // search direction of a cell's neighbours on the fly from z and the old p.
     R *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *p2 = nullptr, *q = nullptr;
+    // The preconditioner cycle captured as a CUDA graph, one per r.z slot, with
+    // the kernels it holds and the event pairs of the kernel-class timers
+    // recorded inside it (captured with timing mask cyc_mask).
+    static constexpr int MAX_CYC_TIMERS = 256;
+    cudaGraphExec_t cyc[2] = {nullptr, nullptr};
+    long long cyc_kernels[2] = {0, 0};
+    int cyc_ntimers[2] = {0, 0};
+    int cyc_cls[2][MAX_CYC_TIMERS] = {};
+    cudaEvent_t cyc_ev[2][2 * MAX_CYC_TIMERS] = {};
+    unsigned cyc_mask = 0;
 };
 
 }  // namespace wpf
@@ -139,6 +149,16 @@ struct wpf_handle {
     cudaEvent_t pend_ev[512];
     double kt_ms[16];
     long long kt_count[16];
+    // timers while a graph is being captured (event record nodes: cap_ev is
+    // non-null only during a capture) and the pairs of launched graphs still
+    // to be read
+    int* cap_ntimers;
+    int* cap_cls;
+    cudaEvent_t* cap_ev;
+    int cap_max;
+    int ngpend;
+    int gpend_cls[512];
+    cudaEvent_t gpend_a[512], gpend_b[512];
 };
 
 namespace wpf {
@@ -317,6 +337,7 @@ int phys_set_dirichlet(wpf_handle* h);
 int phys_reduce(wpf_handle* h, wpf_diag* d);
 int solver_setup(wpf_handle* h);
 int solver_free(wpf_handle* h);
+void solver_drop_graphs(wpf_handle* h);   // after an options change
 int solve_pressure(wpf_handle* h, wpf_step_stats* st);
 
 int ensure_per_routine_arrays(wpf_handle* h);

@@ -692,7 +692,14 @@ static int alloc_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
 }
 
 template <typename R>
+static void drop_cycles(Hierarchy<R>& H);
+template <typename R>
+static void free_cycle_events(Hierarchy<R>& H);
+
+template <typename R>
 static void free_hierarchy(Hierarchy<R>& H) {
+    drop_cycles(H);
+    free_cycle_events(H);
     for (int l = 0; l < H.nlev; ++l) {
         Level<R>& L = H.lv[l];
         cudaFree(L.cx); cudaFree(L.cy); cudaFree(L.cz); cudaFree(L.diag); cudaFree(L.idiag);
@@ -835,6 +842,83 @@ static void vcycle(wpf_handle* h, Hierarchy<R>& H, int nu, double* rz) {
     }
 }
 
+template <typename R>
+static void drop_cycles(Hierarchy<R>& H) {
+    for (int c = 0; c < 2; ++c) {
+        if (H.cyc[c]) cudaGraphExecDestroy(H.cyc[c]);
+        H.cyc[c] = nullptr;
+        H.cyc_kernels[c] = 0;
+        H.cyc_ntimers[c] = 0;
+    }
+}
+
+template <typename R>
+static void free_cycle_events(Hierarchy<R>& H) {
+    for (int c = 0; c < 2; ++c)
+        for (int e = 0; e < 2 * Hierarchy<R>::MAX_CYC_TIMERS; ++e)
+            if (H.cyc_ev[c][e]) { cudaEventDestroy(H.cyc_ev[c][e]); H.cyc_ev[c][e] = nullptr; }
+}
+
+// One preconditioner cycle accumulating r.z into rz slot `slot` (0 or 1).
+// The cycle launches tens of small kernels on the coarse levels, so it is
+// captured once per slot as a CUDA graph and replayed: the same kernels with
+// the same arguments in the same order (the hierarchy's buffers are fixed and
+// its coefficients are rebuilt in place every solve).  Kernel-class timers
+// become event record nodes of the graph, folded in after each replay.
+template <typename R>
+static int run_cycle(wpf_handle* h, Hierarchy<R>& H, int nu, int slot) {
+    double* rz = h->dsc + S_RZ0 + slot;
+    if (h->opts.flags & WPF_SOLVER_NO_GRAPHS) {
+        vcycle(h, H, nu, rz);
+        WPF_CUDA(cudaGetLastError());
+        return WPF_OK;
+    }
+    if (H.cyc[slot] && H.cyc_mask != h->timing_mask) drop_cycles(H);
+    cudaStream_t s = h->stream;
+    if (!H.cyc[slot]) {
+        if (h->timing_mask && !H.cyc_ev[slot][0])
+            for (int e = 0; e < 2 * Hierarchy<R>::MAX_CYC_TIMERS; ++e)
+                WPF_CUDA(cudaEventCreate(&H.cyc_ev[slot][e]));
+        const long long l0 = h->nlaunch;
+        H.cyc_ntimers[slot] = 0;
+        WPF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        if (h->timing_mask) {
+            h->cap_ntimers = &H.cyc_ntimers[slot];
+            h->cap_cls = H.cyc_cls[slot];
+            h->cap_max = Hierarchy<R>::MAX_CYC_TIMERS;
+            h->cap_ev = H.cyc_ev[slot];
+        }
+        vcycle(h, H, nu, rz);
+        h->cap_ev = nullptr;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e1 = cudaStreamEndCapture(s, &graph);
+        const long long nk = h->nlaunch - l0;
+        h->nlaunch = l0;
+        if (e1 != cudaSuccess || !graph) {
+            cudaGetLastError();
+            return WPF_ERR_CUDA;
+        }
+        const cudaError_t e2 = cudaGraphInstantiate(&H.cyc[slot], graph, 0);
+        cudaGraphDestroy(graph);
+        if (e2 != cudaSuccess) {
+            H.cyc[slot] = nullptr;
+            cudaGetLastError();
+            return WPF_ERR_CUDA;
+        }
+        H.cyc_kernels[slot] = nk;
+        H.cyc_mask = h->timing_mask;
+    }
+    WPF_CUDA(cudaGraphLaunch(H.cyc[slot], s));
+    h->nlaunch += H.cyc_kernels[slot];
+    for (int t = 0; t < H.cyc_ntimers[slot] && h->ngpend < 512; ++t) {
+        h->gpend_cls[h->ngpend] = H.cyc_cls[slot][t];
+        h->gpend_a[h->ngpend] = H.cyc_ev[slot][2 * t];
+        h->gpend_b[h->ngpend] = H.cyc_ev[slot][2 * t + 1];
+        ++h->ngpend;
+    }
+    return WPF_OK;
+}
+
 static int read_slot(wpf_handle* h, int slot, int n = 1) {
     WPF_CUDA(cudaMemcpyAsync(h->hsc + slot, h->dsc + slot, n * sizeof(double), cudaMemcpyDeviceToHost,
                              h->stream));
@@ -861,7 +945,8 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
     *iters = 0;
     *final_ratio = 1.0;
     if (!(r0 > 0.0)) return r0 == 0.0 ? WPF_OK : WPF_ERR_NONFINITE;
-    vcycle(h, H, nu, d + S_RZ0);
+    rc = run_cycle(h, H, nu, 0);
+    if (rc) return rc;
     int cur = 0;          // rz of this iteration in S_RZ0 + cur
     R* pold = H.p2;
     R* pnew = H.p;
@@ -881,7 +966,8 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
         if (rn <= tol * r0) return WPF_OK;
         const int nxt = cur ^ 1;
         WPF_CUDA(cudaMemsetAsync(d + S_RZ0 + nxt, 0, sizeof(double), s));
-        vcycle(h, H, nu, d + S_RZ0 + nxt);
+        rc = run_cycle(h, H, nu, nxt);
+        if (rc) return rc;
         cur = nxt;
         R* t = pold; pold = pnew; pnew = t;
     }
@@ -909,6 +995,11 @@ int solver_setup(wpf_handle* h) {
         return WPF_OK;
     }
     return alloc_hierarchy(h, h->h64);
+}
+
+void solver_drop_graphs(wpf_handle* h) {
+    drop_cycles(h->h64);
+    drop_cycles(h->h32);
 }
 
 int solver_free(wpf_handle* h) {

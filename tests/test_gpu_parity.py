@@ -243,13 +243,33 @@ def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
     out = {}
     for name, thr in (("pipelined", 1), ("half", 1 << 40)):
         with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="fp64",
-                        rtol=1e-12, sweep_min_cells=thr) as sim:
+                        rtol=1e-12, sweep_min_cells=thr, w_from_level=99) as sim:
             sim.calcPermeability()
             st = sim.solvePressure()
             assert st.converged and st.relres <= 1e-12
             out[name] = (st.inner_iterations, sim.download("pressure"))
     assert abs(out["pipelined"][0] - out["half"][0]) <= 1
     assert rel_l2(out["pipelined"][1], out["half"][1]) < 1e-9
+
+
+@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+def test_graph_replay_matches_direct_launches(oracle_mod, solver):
+    """Replaying the captured preconditioner cycle gives the same solve as
+    launching its kernels one by one: same iterations and the same pressure
+    up to the order of the block-sum atomics, over several steps (the graph is
+    captured once and replayed with rebuilt coefficients)."""
+    _, Simulation = _sim_mod()
+    case = _case((96, 64, 48), seed=23, log_var=2.0, corr_len=6.0)
+    p = case.params
+    out = {}
+    for graphs in (True, False):
+        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver=solver,
+                        rtol=1e-10, graphs=graphs) as sim:
+            its = [sim.step().inner_iterations for _ in range(3)]
+            out[graphs] = (its, sim.download("pressure"), sim.download("phase"))
+    assert all(abs(a - b) <= 1 for a, b in zip(out[True][0], out[False][0]))
+    assert rel_l2(out[True][1], out[False][1]) < 1e-9
+    assert rel_l2(out[True][2], out[False][2]) < 1e-9
 
 
 @pytest.mark.parametrize("solver", ["mixed", "fp64"])
