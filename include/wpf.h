@@ -200,7 +200,8 @@ int wpf_launch_count(const wpf_handle* h, int64_t* n);
 /* Per-kernel-class device timers (CUDA events around each launch of the
  * classes in `mask`; bit c = class c): 0 permeability, 1 FP64 residual,
  * 2 solver coefficients, 3 finest-level smoother, 4 other multigrid kernels,
- * 5 PCG operator apply, 6 PCG vector kernels, 7 fused update, 8 other.
+ * 5 PCG operator apply, 6 PCG vector kernels, 7 fused update, 8 other,
+ * 9 single-block bottom cycle of the multigrid hierarchy.
  * Setting the mask resets the totals; wpf_kernel_times returns the summed
  * milliseconds and launch counts of the first n classes.                  */
 int wpf_set_kernel_timing(wpf_handle* h, uint32_t mask);

@@ -473,9 +473,18 @@ struct BottomArgs {
 
 template <typename R>
 struct BLevel {
-    int nx, ny, nz, n;
+    int nx, ny, nz, n, hx;   // hx = cells of one colour per row, at most
+    // q / d = (q * ceil(2^32 / d)) >> 32, exact for q * d < 2^32 (here q, d < 2^13)
+    unsigned long long mnx, mny, mhx;
     R *cx, *cy, *cz, *d, *id, *x, *b;
 };
+
+__host__ __device__ inline unsigned long long div_magic(unsigned d) {
+    return ((1ull << 32) + d - 1) / d;
+}
+__device__ __forceinline__ int fdiv(int q, unsigned long long m) {
+    return (int)(((unsigned long long)(unsigned)q * m) >> 32);
+}
 
 template <typename R>
 __device__ __forceinline__ R b_offsum(const BLevel<R>& L, int c, int i, int j, int k) {
@@ -493,29 +502,33 @@ __device__ __forceinline__ R b_offsum(const BLevel<R>& L, int c, int i, int j, i
 // colour of a 0-based cell in the 1-based convention of the other kernels
 __device__ __forceinline__ int b_colour(int i, int j, int k) { return (i + j + k + 1) & 1; }
 
+// One colour of Gauss-Seidel on a staged level: thread m takes the m-th cell of
+// that colour (row r = (j,k), t-th of the row).  first: the zero-guess first
+// sweep, which also zeroes the other colour (x = 0 before it).
 template <typename R>
-__device__ void b_sweep(const BLevel<R>& L, int color) {
-    for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
-        const int i = c % L.nx, r = c / L.nx, j = r % L.ny, k = r / L.ny;
-        if (b_colour(i, j, k) != color) continue;
-        L.x[c] = L.id[c] * (L.b[c] + b_offsum(L, c, i, j, k));
+__device__ __forceinline__ void b_sweep(const BLevel<R> L, int color, bool first = false) {
+    const int nh = L.hx * L.ny * L.nz;
+    for (int m = threadIdx.x; m < nh; m += blockDim.x) {
+        const int r = fdiv(m, L.mhx), t = m - r * L.hx, k = fdiv(r, L.mny), j = r - k * L.ny;
+        const int par = (color + 1 + j + k) & 1;   // b_colour(i, j, k) == color
+        const int i = 2 * t + par;
+        const int c = i + L.nx * r;
+        if (first) {
+            if (i < L.nx) L.x[c] = L.id[c] * L.b[c];
+            const int io = 2 * t + (par ^ 1);
+            if (io < L.nx) L.x[c - i + io] = 0;
+        } else if (i < L.nx) {
+            L.x[c] = L.id[c] * (L.b[c] + b_offsum(L, c, i, j, k));
+        }
     }
     __syncthreads();
 }
 
+// b of level l+1 = residual of level l summed over each aggregate.
 template <typename R>
-__device__ void b_cycle(const BLevel<R>* lv, int l, int last, int nu) {
-    const BLevel<R>& L = lv[l];
-    for (int c = threadIdx.x; c < L.n; c += blockDim.x) L.x[c] = 0;
-    __syncthreads();
-    if (l == last) {
-        for (int s = 0; s < 8; ++s) { b_sweep(L, 0); b_sweep(L, 1); }
-        return;
-    }
-    for (int s = 0; s < nu; ++s) { b_sweep(L, 0); b_sweep(L, 1); }
-    const BLevel<R>& C = lv[l + 1];
+__device__ __forceinline__ void b_restrict(const BLevel<R> L, const BLevel<R> C) {
     for (int q = threadIdx.x; q < C.n; q += blockDim.x) {
-        const int I = q % C.nx, rr = q / C.nx, J = rr % C.ny, K = rr / C.ny;
+        const int rr = fdiv(q, C.mnx), I = q - rr * C.nx, K = fdiv(rr, C.mny), J = rr - K * C.ny;
         R s = 0;
         for (int dk = 0; dk < 2; ++dk) {
             const int k = 2 * K + dk;
@@ -534,13 +547,49 @@ __device__ void b_cycle(const BLevel<R>* lv, int l, int last, int nu) {
         C.b[q] = s;
     }
     __syncthreads();
-    b_cycle(lv, l + 1, last, nu);
+}
+
+template <typename R>
+__device__ __forceinline__ void b_prolong(const BLevel<R> L, const BLevel<R> C) {
     for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
-        const int i = c % L.nx, r = c / L.nx, j = r % L.ny, k = r / L.ny;
+        const int r = fdiv(c, L.mnx), i = c - r * L.nx, k = fdiv(r, L.mny), j = r - k * L.ny;
         if (L.id[c] != (R)0) L.x[c] += C.x[(i >> 1) + C.nx * ((j >> 1) + C.ny * (k >> 1))];
     }
     __syncthreads();
-    for (int s = 0; s < nu; ++s) { b_sweep(L, 1); b_sweep(L, 0); }
+}
+
+// V-cycle over the staged levels l0..last, written as two loops (no device
+// recursion, so no call stack): nu symmetric red-black sweeps around each
+// coarse correction.  The coarsest level (at most 2 cells per axis) is one
+// cell in the usual case, solved exactly; otherwise it gets 4 symmetric
+// red-black sweep pairs from zero -- a symmetric operator, like the rest.
+template <typename R>
+__device__ void b_vcycle(const BLevel<R>* lv, int l0, int last, int nu) {
+    for (int l = l0; l < last; ++l) {
+        const BLevel<R> L = lv[l];
+        b_sweep(L, 0, true);
+        b_sweep(L, 1);
+        for (int s = 1; s < nu; ++s) { b_sweep(L, 0); b_sweep(L, 1); }
+        b_restrict(L, lv[l + 1]);
+    }
+    {
+        const BLevel<R> L = lv[last];
+        if (L.n == 1) {
+            if (threadIdx.x == 0) L.x[0] = L.id[0] * L.b[0];
+            __syncthreads();
+        } else {
+            b_sweep(L, 0, true);
+            b_sweep(L, 1);
+            b_sweep(L, 1);
+            b_sweep(L, 0);
+            for (int s = 1; s < 4; ++s) { b_sweep(L, 0); b_sweep(L, 1); b_sweep(L, 1); b_sweep(L, 0); }
+        }
+    }
+    for (int l = last - 1; l >= l0; --l) {
+        const BLevel<R> L = lv[l];
+        b_prolong(L, lv[l + 1]);
+        for (int s = 0; s < nu; ++s) { b_sweep(L, 1); b_sweep(L, 0); }
+    }
 }
 
 template <typename R>
@@ -554,6 +603,10 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(BottomArgs<R> A) {
             const Grid& g = A.lv[l].g;
             BLevel<R>& B = lv[l];
             B.nx = g.nx; B.ny = g.ny; B.nz = g.nz; B.n = g.nx * g.ny * g.nz;
+            B.hx = (g.nx + 1) / 2;
+            B.mnx = div_magic(g.nx);
+            B.mny = div_magic(g.ny);
+            B.mhx = div_magic(B.hx);
             R** arrs[7] = {&B.cx, &B.cy, &B.cz, &B.d, &B.id, &B.x, &B.b};
             for (auto a : arrs) { *a = p; p += B.n; }
         }
@@ -561,21 +614,22 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom(BottomArgs<R> A) {
     __syncthreads();
     for (int l = A.l0; l < A.nlev; ++l) {   // stage the operators and the top right-hand side
         const Level<R>& G = A.lv[l];
-        const BLevel<R>& B = lv[l];
+        const BLevel<R> B = lv[l];
         for (int c = threadIdx.x; c < B.n; c += blockDim.x) {
-            const int i = c % B.nx, r = c / B.nx, j = r % B.ny, k = r / B.ny;
+            const int r = fdiv(c, B.mnx), i = c - r * B.nx, k = fdiv(r, B.mny), j = r - k * B.ny;
             const long long n = G.g.at(i + 1, j + 1, k + 1);
-            B.cx[c] = G.cx[n]; B.cy[c] = G.cy[n]; B.cz[c] = G.cz[n];
-            B.d[c] = G.diag[n]; B.id[c] = G.idiag[n];
-            if (l == A.l0) B.b[c] = G.b[n];
+            const R vx = G.cx[n], vy = G.cy[n], vz = G.cz[n], vd = G.diag[n], vi = G.idiag[n];
+            const R vb = l == A.l0 ? G.b[n] : (R)0;
+            B.cx[c] = vx; B.cy[c] = vy; B.cz[c] = vz; B.d[c] = vd; B.id[c] = vi;
+            if (l == A.l0) B.b[c] = vb;
         }
     }
     __syncthreads();
-    b_cycle(lv, A.l0, A.nlev - 1, A.nu);
+    b_vcycle(lv, A.l0, A.nlev - 1, A.nu);
     const Level<R>& G = A.lv[A.l0];
-    const BLevel<R>& B = lv[A.l0];
+    const BLevel<R> B = lv[A.l0];
     for (int c = threadIdx.x; c < B.n; c += blockDim.x) {
-        const int i = c % B.nx, r = c / B.nx, j = r % B.ny, k = r / B.ny;
+        const int r = fdiv(c, B.mnx), i = c - r * B.nx, k = fdiv(r, B.mny), j = r - k * B.ny;
         G.x[G.g.at(i + 1, j + 1, k + 1)] = B.x[c];
     }
 }
@@ -761,7 +815,7 @@ static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, l
         A.nlev = H.nlev;
         A.nu = nu;
         for (int q = 0; q < H.nlev; ++q) A.lv[q] = H.lv[q];
-        WPF_LAUNCH(h, lb == 0 ? KC_SMOOTH0 : KC_MGREST,
+        WPF_LAUNCH(h, lb == 0 ? KC_SMOOTH0 : KC_BOTTOM,
                    k_bottom<R><<<1, BOTTOM_THREADS, bottom_smem(H, lb), s>>>(A));
         return;
     }
