@@ -89,6 +89,15 @@ typedef struct wpf_solver_opts {
 } wpf_solver_opts;
 
 #define WPF_SOLVER_NO_GRAPHS 1
+/* WPF_SOLVER_EXTRAPOLATE: start each solve from p + e, e extrapolated in time
+ * from the pressure increments of the last two solves (quadratic in t with the
+ * step sizes wpf_step knows; equal steps assumed by wpf_solve_pressure), and
+ * fall back to the previous pressure (the reference's x0, wPFAW3D.f90:980)
+ * whenever p + e has the larger FP64 residual.  The solve still ends at the
+ * same rtol on the true FP64 residual, so only the iteration count changes.
+ * The increment history survives wpf_upload and is cleared by wpf_set_wells
+ * and wpf_set_solver.  No counterpart in the reference.                    */
+#define WPF_SOLVER_EXTRAPOLATE 2
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {
@@ -103,7 +112,8 @@ typedef struct wpf_step_stats {
     double solve_ms;           /* device time of the Darcy solve                       */
     double update_ms;          /* device time of the fused update kernel               */
     int32_t kernel_launches;   /* kernels this call launched                           */
-    int32_t pad;
+    int32_t warm_start;        /* 1: the solve started from the extrapolated p + e;
+                                  -1: it was tried and rejected; 0: not tried         */
     double relres0;            /* relative residual of the warm start                  */
 } wpf_step_stats;
 

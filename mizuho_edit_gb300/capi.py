@@ -24,7 +24,8 @@ NOALLOC_MAX_PLANES = 4096
 
 SOLVER_FP64 = 0
 SOLVER_MIXED = 1
-SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bit
+SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bits
+SOLVER_EXTRAPOLATE = 2
 
 
 class WpfError(RuntimeError):
@@ -59,7 +60,8 @@ class StepStats(C.Structure):
                 ("converged", C.c_int32), ("overshoot_cells", C.c_int32), ("relres", C.c_double),
                 ("taumin", C.c_double), ("dtime", C.c_double), ("max_courant", C.c_double),
                 ("solve_ms", C.c_double), ("update_ms", C.c_double),
-                ("kernel_launches", C.c_int32), ("pad", C.c_int32), ("relres0", C.c_double)]
+                ("kernel_launches", C.c_int32), ("warm_start", C.c_int32),
+                ("relres0", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

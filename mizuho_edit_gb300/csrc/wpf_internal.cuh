@@ -51,6 +51,7 @@ enum Slot {
     S_UMAX_BITS,        // max |u| (bits of a non-negative double)
     S_RR64,             // ||r||^2 of the FP64 residual
     S_BB64,             // ||b||^2 of the reference right-hand side
+    S_RR0WS,            // ||r(p)||^2 when the solve tries an extrapolated start
     S_PQ,               // PCG p.q
     S_RR,               // PCG r.r
     S_RZ0, S_RZ1,       // PCG r.z (double buffered)
@@ -128,6 +129,13 @@ struct wpf_handle {
     wpf::Hierarchy<double> h64;
     wpf::Hierarchy<float> h32;
     double* r64;             // FP64 residual (mixed mode)
+    // extrapolated warm start (WPF_SOLVER_EXTRAPOLATE): the pressure increments
+    // of the last two solves (ws[0] newest) and this solve's (ws[2]), FP32
+    float* ws[3];
+    int ws_hist;             // increments held (0..2)
+    int ws_used;             // this solve started from p + e
+    double ws_hn, ws_h1, ws_h2;   // step sizes: this step, previous, one before (0 = unknown)
+    long long ws_fallbacks;  // solves whose extrapolated start was rejected
     double* dsc;             // device scalar slots
     double* hsc;             // pinned host mirror of the scalar slots
     double* partials;        // per-block partial sums of the diagnostics

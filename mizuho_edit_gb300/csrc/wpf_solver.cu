@@ -106,6 +106,95 @@ __global__ void __launch_bounds__(RB) k_add_correction(Grid g, double* __restric
     }
 }
 
+// ---- extrapolated warm start ------------------------------------------------
+// e = a d1 + b d2 from the last two increments, rounded the same way in every
+// kernel that forms it.
+__device__ __forceinline__ float ws_ext(const float* __restrict__ d1, const float* __restrict__ d2,
+                                        float a, float b, long long n) {
+    return __fmaf_rn(a, d1[n], __fmul_rn(b, d2[n]));
+}
+
+// Pass-0 residual of the start p + e: r0 = r(p) in FP64 exactly as
+// k_resid64 (||r0||^2 into S_RR0WS, ||b_ref||^2 into S_BB64), then
+// r1 = r0 - A'e with A'e from the level-0 coefficients in precision R (e is a
+// small increment, so its rounding stays orders of magnitude below the outer
+// tolerance); writes r1 and dnew = e, accumulates ||r1||^2 into S_RR64.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restrict__ pr,
+                                                   const double* __restrict__ Tx,
+                                                   const double* __restrict__ Ty,
+                                                   const double* __restrict__ Tz,
+                                                   const uint8_t* __restrict__ fl,
+                                                   const double* __restrict__ qterm,
+                                                   const R* __restrict__ cx, const R* __restrict__ cy,
+                                                   const R* __restrict__ cz,
+                                                   const R* __restrict__ diag,
+                                                   const float* __restrict__ d1,
+                                                   const float* __restrict__ d2, float a, float b,
+                                                   R* __restrict__ rout, float* __restrict__ dnew,
+                                                   double* dsc) {
+    double rr1 = 0.0, rr0 = 0.0, bb = 0.0;
+    const long long sy = g.P, sz = g.S;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        const uint8_t f = fl[n];
+        const double p0 = pr[n];
+        double r0 = 0.0, r1 = 0.0;
+        float e = 0.f;
+        if (f & F_DIR) {
+            bb += p0 * p0;
+        } else {
+            const double q = qterm ? qterm[n] : 0.0;
+            const double txp = Tx[n], txm = Tx[n - 1], typ = Ty[n], tym = Ty[n - sy];
+            const double tzp = Tz[n], tzm = Tz[n - sz];
+            const double pxp = pr[n + 1], pxm = pr[n - 1], pyp = pr[n + sy], pym = pr[n - sy];
+            const double pzp = pr[n + sz], pzm = pr[n - sz];
+            r0 = q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
+                      typ * (pyp - p0) + tzp * (pzp - p0));
+            double bref = -q;
+            if (fl[n - sz] & F_DIR) bref -= pzm * tzm;
+            if (fl[n - sy] & F_DIR) bref -= pym * tym;
+            if (fl[n - 1] & F_DIR) bref -= pxm * txm;
+            if (fl[n + 1] & F_DIR) bref -= pxp * txp;
+            if (fl[n + sy] & F_DIR) bref -= pyp * typ;
+            if (fl[n + sz] & F_DIR) bref -= pzp * tzp;
+            bb += bref * bref;
+            e = ws_ext(d1, d2, a, b, n);
+            const R ae = diag[n] * (R)e -
+                         (cx[n] * (R)ws_ext(d1, d2, a, b, n + 1) + cx[n - 1] * (R)ws_ext(d1, d2, a, b, n - 1) +
+                          cy[n] * (R)ws_ext(d1, d2, a, b, n + sy) + cy[n - sy] * (R)ws_ext(d1, d2, a, b, n - sy) +
+                          cz[n] * (R)ws_ext(d1, d2, a, b, n + sz) + cz[n - sz] * (R)ws_ext(d1, d2, a, b, n - sz));
+            r1 = r0 - (double)ae;
+        }
+        rout[n] = (R)r1;
+        dnew[n] = e;
+        rr1 += r1 * r1;
+        rr0 += r0 * r0;
+    }
+    block_add(rr1, dsc + S_RR64);
+    block_add(rr0, dsc + S_RR0WS);
+    block_add(bb, dsc + S_BB64);
+}
+
+// p += e (add_ext: the extrapolated start, added once) + x (the pass's
+// correction, when x != null); dnew accumulates x, so that after the last
+// pass it holds this solve's whole increment.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_add_correction_ws(Grid g, double* __restrict__ pr,
+                                                          const R* __restrict__ x,
+                                                          const float* __restrict__ d1,
+                                                          const float* __restrict__ d2, float a,
+                                                          float b, int add_ext,
+                                                          float* __restrict__ dnew) {
+    ROW_LOOP_U4(g) {
+        const long long n = g.at(i, j, k);
+        double inc = x ? (double)x[n] : 0.0;
+        if (add_ext) inc += (double)ws_ext(d1, d2, a, b, n);
+        pr[n] += inc;
+        if (x) dnew[n] += (float)x[n];
+    }
+}
+
 // Level-0 coefficients of A' from T and the Dirichlet flags.
 template <typename R>
 __global__ void __launch_bounds__(RB) k_l0_coeffs(Grid g, const double* __restrict__ Tx,
@@ -1042,6 +1131,11 @@ static int set_sweep_smem() {
 int solver_setup(wpf_handle* h) {
     int rc = h->opts.mode == WPF_SOLVER_MIXED ? set_sweep_smem<float>() : set_sweep_smem<double>();
     if (rc) return rc;
+    if ((h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && !h->ws[0]) {
+        for (int q = 0; q < 3; ++q)
+            if ((rc = dev_alloc(h, (void**)&h->ws[q], sizeof(float) * h->g.total))) return rc;
+        h->ws_hist = 0;
+    }
     if (h->opts.mode == WPF_SOLVER_MIXED) {
         rc = alloc_hierarchy(h, h->h32);
         if (rc) return rc;
@@ -1061,7 +1155,36 @@ int solver_free(wpf_handle* h) {
     free_hierarchy(h->h32);
     if (h->r64) cudaFree(h->r64);
     h->r64 = nullptr;
+    for (int q = 0; q < 3; ++q) {
+        if (h->ws[q]) cudaFree(h->ws[q]);
+        h->ws[q] = nullptr;
+    }
+    h->ws_hist = 0;
     return WPF_OK;
+}
+
+// Coefficients of e = a d1 + b d2: the Newton form of the quadratic through
+// the last three pressures in time, evaluated one step hn ahead,
+//   e = (hn/h1) d1 + hn (hn + h1) / (h1 + h2) (d1/h1 - d2/h2),
+// (linear, e = (hn/h1) d1, with one increment; equal steps when a step size
+// is unknown: 2 d1 - d2, d1).
+static void ws_coeffs(const wpf_handle* h, float* a, float* b) {
+    *a = 0.f;
+    *b = 0.f;
+    if (h->ws_hist <= 0) return;
+    const double hn = h->ws_hn, h1 = h->ws_h1, h2 = h->ws_h2;
+    if (h->ws_hist == 1) {
+        *a = (hn > 0 && h1 > 0) ? (float)(hn / h1) : 1.f;
+        return;
+    }
+    if (!(hn > 0 && h1 > 0 && h2 > 0)) {
+        *a = 2.f;
+        *b = -1.f;
+        return;
+    }
+    const double c = hn * (hn + h1) / (h1 + h2);
+    *a = (float)(hn / h1 + c / h1);
+    *b = (float)(-c / h2);
 }
 
 template <typename R>
@@ -1075,19 +1198,60 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     const int nu = h->opts.smooth_sweeps > 0 ? h->opts.smooth_sweeps : 2;
     int outer = 0, inner_total = 0, status = WPF_ERR_NOT_CONVERGED;
     double relres = 0.0, bnorm = 0.0, relres0 = 0.0;
+    // extrapolated start: tried on pass 0 when two (or one) increments are held
+    const bool ws_on = (h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && h->ws[0];
+    float wa = 0.f, wb = 0.f;
+    if (ws_on) ws_coeffs(h, &wa, &wb);
+    float *d1 = ws_on ? h->ws[0] : nullptr, *d2 = ws_on ? h->ws[1] : nullptr;
+    float* dnew = ws_on ? h->ws[2] : nullptr;
+    bool ext_pending = false;   // e accepted but not yet added to the pressure
+    h->ws_used = 0;
     for (int pass = 0; pass <= h->opts.max_outer; ++pass) {
-        WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 2 * sizeof(double), s));
-        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                          h->flags, h->qterm, H.r, h->dsc, pass == 0));
-        WPF_CUDA(cudaGetLastError());
-        rc = read_slot(h, S_RR64, 2);
-        if (rc) return rc;
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 3 * sizeof(double), s));   // RR64, BB64, RR0WS
+        bool plain = true;
+        if (pass == 0 && ws_on && h->ws_hist > 0) {
+            WPF_LAUNCH(h, KC_RESID64, k_resid64_ws<R><<<rb, RB, 0, s>>>(
+                g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, H.lv[0].cx, H.lv[0].cy,
+                H.lv[0].cz, H.lv[0].diag, d1, d2, wa, wb, H.r, dnew, h->dsc));
+            WPF_CUDA(cudaGetLastError());
+            rc = read_slot(h, S_RR64, 3);
+            if (rc) return rc;
+            const double r1 = h->hsc[S_RR64], r0 = h->hsc[S_RR0WS];
+            if (r1 <= r0 && r1 == r1) {   // the fallback rule: keep p + e only if it is better
+                plain = false;
+                ext_pending = true;
+                h->ws_used = 1;
+            } else {
+                h->ws_used = -1;
+                ++h->ws_fallbacks;
+                WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 3 * sizeof(double), s));
+            }
+        }
+        if (plain) {
+            if (pass == 0 && ws_on) WPF_CUDA(cudaMemsetAsync(dnew, 0, sizeof(float) * g.total, s));
+            WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+                                                              h->flags, h->qterm, H.r, h->dsc, pass == 0));
+            WPF_CUDA(cudaGetLastError());
+            rc = read_slot(h, S_RR64, 2);
+            if (rc) return rc;
+        }
         if (pass == 0) bnorm = sqrt(h->hsc[S_BB64]);
         const double rnorm = sqrt(h->hsc[S_RR64]);
         relres = bnorm > 0.0 ? rnorm / bnorm : rnorm;
         if (pass == 0) relres0 = relres;
         if (!(relres == relres) || isinf(relres)) { status = WPF_ERR_NONFINITE; break; }
-        if (relres <= h->opts.rtol) { status = WPF_OK; break; }
+        if (relres <= h->opts.rtol) {
+            // an extrapolated start whose (partly FP32-evaluated) residual
+            // already meets rtol is added to p and verified by a plain FP64 pass
+            if (ext_pending && pass < h->opts.max_outer) {
+                WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(
+                    g, h->pressure, (const R*)nullptr, d1, d2, wa, wb, 1, dnew));
+                ext_pending = false;
+                continue;
+            }
+            status = WPF_OK;
+            break;
+        }
         if (pass == h->opts.max_outer) break;
         outer = pass + 1;
         double want = 0.5 * h->opts.rtol / relres;
@@ -1097,8 +1261,29 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         rc = pcg<R>(h, H, tol, h->opts.max_inner, nu, &its, &ratio);
         inner_total += its;
         if (rc == WPF_ERR_NONFINITE) { status = rc; break; }
-        WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x));
+        if (ws_on)
+            WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x, d1, d2, wa,
+                                                                           wb, ext_pending, dnew));
+        else
+            WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x));
+        ext_pending = false;
         WPF_CUDA(cudaGetLastError());
+    }
+    if (ext_pending)   // max_outer = 0: the start was accepted but never verified
+        WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(g, h->pressure, (const R*)nullptr,
+                                                                       d1, d2, wa, wb, 1, dnew));
+    if (ws_on) {
+        if (status == WPF_OK) {   // this increment becomes the newest of the history
+            float* t = h->ws[1];
+            h->ws[1] = h->ws[0];
+            h->ws[0] = h->ws[2];
+            h->ws[2] = t;
+            h->ws_hist = h->ws_hist < 2 ? h->ws_hist + 1 : 2;
+            h->ws_h2 = h->ws_h1;
+            h->ws_h1 = h->ws_hn;
+        } else {
+            h->ws_hist = 0;
+        }
     }
     if (st) {
         st->outer_iterations = outer;
@@ -1106,6 +1291,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         st->converged = status == WPF_OK;
         st->relres = relres;
         st->relres0 = relres0;
+        st->warm_start = h->ws_used;
     }
     return status;
 }

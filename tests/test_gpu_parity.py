@@ -47,12 +47,13 @@ def _rough_state(case, seed=5, overshoot=0.0):
     return case
 
 
-def _pair(case, solver="fp64", rtol=1e-13):
+def _pair(case, solver="fp64", rtol=1e-13, **kw):
     import oracle as O
     capi, Simulation = _sim_mod()
     p = case.params
     ref = O.OracleSim(p, case.permeab_rock, case.phase, case.concent)
-    sim = Simulation(p, case.permeab_rock, case.phase, case.concent, solver=solver, rtol=rtol)
+    sim = Simulation(p, case.permeab_rock, case.phase, case.concent, solver=solver, rtol=rtol,
+                     **kw)
     return ref, sim
 
 
@@ -184,10 +185,12 @@ def test_fp64_100_steps(oracle_mod, n, steps):
         assert dg[k] == pytest.approx(rd[k], rel=1e-9, abs=1e-12), k
 
 
-def test_mixed_100_steps(oracle_mod):
-    """Mixed form at a 1e-8 Darcy residual: pressure within 1e-6 of the oracle."""
+@pytest.mark.parametrize("extrapolate", [False, True])
+def test_mixed_100_steps(oracle_mod, extrapolate):
+    """Mixed form at a 1e-8 Darcy residual, from the previous or the
+    time-extrapolated pressure: fields within 1e-6 of the oracle."""
     case = _case((24, 20, 16), seed=12, log_var=2.0, corr_len=4.0)
-    ref, sim = _pair(case, solver="mixed", rtol=1e-8)
+    ref, sim = _pair(case, solver="mixed", rtol=1e-8, extrapolate=extrapolate)
     with sim:
         for _ in range(100):
             st = sim.step()
@@ -250,6 +253,55 @@ def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
             out[name] = (st.inner_iterations, sim.download("pressure"))
     assert abs(out["pipelined"][0] - out["half"][0]) <= 1
     assert rel_l2(out["pipelined"][1], out["half"][1]) < 1e-9
+
+
+def test_extrapolated_start_same_solution_fewer_iterations(oracle_mod):
+    """The time-extrapolated start changes only where each solve begins: over
+    30 steps the fields agree with the run from the previous pressure to the
+    solver tolerance, every solve still meets rtol on the FP64 residual, and
+    past the start-up transient (the dt jump at step 3, the first front
+    motion) the start is taken and saves iterations."""
+    _, Simulation = _sim_mod()
+    case = _case((96, 64, 64), seed=24, log_var=2.0, corr_len=6.0)
+    p = case.params
+    out = {}
+    for ext in (False, True):
+        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                        rtol=1e-8, extrapolate=ext) as sim:
+            st = [sim.step() for _ in range(30)]
+            assert all(s.converged and s.relres <= 1e-8 for s in st)
+            out[ext] = (st, sim.download("pressure", "phase", "concent"))
+    plain, extr = out[False][0], out[True][0]
+    assert all(s.warm_start == 0 for s in plain)
+    assert extr[0].warm_start == 0                       # no history yet
+    late = slice(18, 30)
+    used = [s.warm_start == 1 for s in extr[late]]
+    assert sum(used) >= len(used) - 1
+    assert sum(s.inner_iterations for s in extr[late]) < sum(s.inner_iterations for s in plain[late])
+    assert (sum(s.relres0 for s in extr[late] if s.warm_start == 1)
+            < 0.2 * sum(s.relres0 for s, u in zip(plain[late], used) if u))
+    for name in ("pressure", "phase", "concent"):
+        assert rel_l2(out[True][1][name], out[False][1][name]) < 1e-6, name
+
+
+def test_extrapolated_start_falls_back(oracle_mod):
+    """A start that would raise the residual is rejected: the solve starts from
+    the stored pressure instead (warm_start = -1) and still converges."""
+    _, Simulation = _sim_mod()
+    case = _case((64, 48, 40), seed=25, log_var=1.5, corr_len=5.0)
+    p = case.params
+    with Simulation(p, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                    rtol=1e-8, extrapolate=True) as sim:
+        hist = []
+        for _ in range(6):
+            hist.append(sim.download("pressure"))
+            sim.step()
+        pn = sim.download("pressure")
+        # move the stored pressure far past the extrapolation: p + e overshoots more
+        sim.upload(pressure=pn + 40.0 * (pn - hist[-1]))
+        st = sim.step()
+        assert st.warm_start == -1
+        assert st.converged and st.relres <= 1e-8
 
 
 @pytest.mark.parametrize("solver", ["mixed", "fp64"])
