@@ -119,7 +119,7 @@ static void free_all(wpf_handle* h) {
     double* d[] = {h->krock, h->phase, h->concent, h->pressure, h->phase_n, h->concent_n,
                    h->T[0], h->T[1], h->T[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
                    h->vel[0], h->vel[1], h->vel[2], h->dphasedt, h->dconcentdt, h->dir_val,
-                   h->qterm, h->dsc, h->partials};
+                   h->qterm, h->dsc, h->partials, h->staging};
     for (double* p : d)
         if (p) cudaFree(p);
     if (h->flags) cudaFree(h->flags);
@@ -307,19 +307,49 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
     return phys_set_dirichlet(h);
 }
 
+// Host fields are dense halo arrays (nx+2)(ny+2)(nz+2) in Fortran order; the
+// device rows are pitched.  A field crosses the host link as one contiguous
+// copy through a dense staging buffer and is re-pitched on the device (block
+// = one row of nx+2 values): row-by-row 2D copies of 2 KB rows run far below
+// the link's bandwidth.
+__global__ void k_repitch(Grid g, const double* __restrict__ src, double* __restrict__ dst,
+                          int to_pitched) {
+    const int w = g.nx + 2;
+    const long long row = blockIdx.x;
+    const long long dense = row * w, pitched = g.at(0, 0, 0) + row * g.P;
+    for (int i = threadIdx.x; i < w; i += blockDim.x) {
+        if (to_pitched) dst[pitched + i] = src[dense + i];
+        else dst[dense + i] = src[pitched + i];
+    }
+}
+
+static int ensure_staging(wpf_handle* h) {
+    if (h->staging) return WPF_OK;
+    const Grid& g = h->g;
+    return dev_alloc(h, (void**)&h->staging, sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2));
+}
+
 static int copy_field_in(wpf_handle* h, double* dst, const double* src) {
     const Grid& g = h->g;
-    WPF_CUDA(cudaMemcpy2DAsync(dst + g.at(0, 0, 0), g.P * sizeof(double), src,
-                               (g.nx + 2) * sizeof(double), (g.nx + 2) * sizeof(double),
-                               (size_t)(g.ny + 2) * (g.nz + 2), cudaMemcpyHostToDevice, h->stream));
+    int rc = ensure_staging(h);
+    if (rc) return rc;
+    const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    WPF_CUDA(cudaMemcpyAsync(h->staging, src, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+        g, h->staging, dst, 1));
+    WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
 
 static int copy_field_out(wpf_handle* h, double* dst, const double* src) {
     const Grid& g = h->g;
-    WPF_CUDA(cudaMemcpy2DAsync(dst, (g.nx + 2) * sizeof(double), src + g.at(0, 0, 0),
-                               g.P * sizeof(double), (g.nx + 2) * sizeof(double),
-                               (size_t)(g.ny + 2) * (g.nz + 2), cudaMemcpyDeviceToHost, h->stream));
+    int rc = ensure_staging(h);
+    if (rc) return rc;
+    const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+        g, src, h->staging, 0));
+    WPF_CUDA(cudaGetLastError());
+    WPF_CUDA(cudaMemcpyAsync(dst, h->staging, G * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return WPF_OK;
 }
 

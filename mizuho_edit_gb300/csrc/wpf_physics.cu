@@ -378,7 +378,10 @@ __device__ __forceinline__ void write_halo_of(const Grid& g, int i, int j, int k
 //   k_update_split  -- every cell: a cell with a bitwise-uniform phase
 //       neighbourhood (dphi/dt = 0, tau = tau0) that is a well or has an
 //       all-zero concentration neighbourhood (dc/dt = 0) is copied to the new
-//       buffers; every other cell is appended to a work list (warp-aggregated).
+//       buffers; every other cell is appended to a work list (warp-aggregated):
+//       interface cells (non-uniform phase) from the front, cells that only
+//       need the concentration rate (uniform phase) from the back, so that no
+//       warp mixes the long phase-rate path with the short one.
 //   k_update_active -- the work list, densely packed into full warps: face
 //       velocities from T = K_f/mu and the solved pressure (zero on the global
 //       boundary faces, as the reference's halo copy makes them), the phase
@@ -394,11 +397,13 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
                                                      int* __restrict__ work, int* nwork,
                                                      double tau0, double* dsc) {
     const long long sy = g.P, sz = g.S;
+    const long long cap = (long long)g.nx * g.ny * g.nz;   // work[] entries
     int any_copy = 0;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const bool well = (fl[n] & F_WELL) != 0;
-        const bool copy = phase_uniform(ph, n, sy, sz) && (well || concent_zero(cc, n, sy, sz));
+        const bool uni = phase_uniform(ph, n, sy, sz);
+        const bool copy = uni && (well || concent_zero(cc, n, sy, sz));
         if (copy) {
             const double a = ph[n], c = cc[n];
             ph_out[n] = a;
@@ -408,14 +413,22 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
             any_copy = 1;
         }
         const unsigned am = __activemask();
-        const unsigned m = __ballot_sync(am, !copy);
-        if (m) {
-            const int lane = threadIdx.x & 31;
-            const int leader = __ffs(m) - 1;
+        const int lane = threadIdx.x & 31;
+        const unsigned ma = __ballot_sync(am, !uni);          // interface cells
+        const unsigned mb = __ballot_sync(am, uni && !copy);  // concentration-only cells
+        if (ma) {
+            const int leader = __ffs(ma) - 1;
             int base = 0;
-            if (lane == leader) base = atomicAdd(nwork, __popc(m));
+            if (lane == leader) base = atomicAdd(nwork, __popc(ma));
             base = __shfl_sync(am, base, leader);
-            if (!copy) work[base + __popc(m & ((1u << lane) - 1))] = (int)n;
+            if (!uni) work[base + __popc(ma & ((1u << lane) - 1))] = (int)n;
+        }
+        if (mb) {
+            const int leader = __ffs(mb) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(nwork + 1, __popc(mb));
+            base = __shfl_sync(am, base, leader);
+            if (uni && !copy) work[cap - 1 - (base + __popc(mb & ((1u << lane) - 1)))] = (int)n;
         }
     }
     if (__syncthreads_or(any_copy) && threadIdx.x == 0)
@@ -439,9 +452,11 @@ __global__ void __launch_bounds__(RB) k_update_active(Grid g, const Phys* __rest
     double taum = 1.0e308, umax = 0.0;
     int overs = 0;
     const long long sy = g.P, sz = g.S;
-    const int nw = *nwork;
+    const long long cap = (long long)g.nx * g.ny * g.nz;
+    const int na = nwork[0], nw = na + nwork[1];
     for (int q = blockIdx.x * RB + threadIdx.x; q < nw; q += gridDim.x * RB) {
-        const long long n = work[q];
+        const bool uni = q >= na;   // from the back: uniform phase, concentration only
+        const long long n = uni ? work[cap - 1 - (q - na)] : work[q];
         const long long r = n - XOFF;
         const int k = (int)(r / g.S);
         const long long r2 = r - (long long)k * g.S;
@@ -464,9 +479,9 @@ __global__ void __launch_bounds__(RB) k_update_active(Grid g, const Phys* __rest
         };
         const bool well = (fl[n] & F_WELL) != 0;
         const double conc = cc[n];
-        double rate, tau;
-        int over;
-        phase_cell(ph, n, sy, sz, vel, conc, well, P, rate, tau, over);
+        double rate = 0.0, tau = P.tau0;
+        int over = 0;
+        if (!uni) phase_cell(ph, n, sy, sz, vel, conc, well, P, rate, tau, over);
         double crate;
         if (well) crate = 0.0;
         else if (concent_zero(cc, n, sy, sz)) crate = P.alpha * rate;
@@ -721,9 +736,9 @@ int phys_fused_update(wpf_handle* h, double dtime, double* taumin, int32_t* over
     WPF_CUDA(cudaMemcpyAsync(&h->hsc[S_NWORK], h->dsc + S_NWORK, sizeof(double),
                              cudaMemcpyDeviceToHost, h->stream));
     rc = read_step_slots(h, taumin, overshoot, umax);
-    int nw;
-    memcpy(&nw, &h->hsc[S_NWORK], sizeof(int));
-    h->last_active = nw;
+    int nw[2];   // interface cells, concentration-only cells (two ints in the slot)
+    memcpy(nw, &h->hsc[S_NWORK], sizeof(nw));
+    h->last_active = nw[0] + nw[1];
     return rc;
 }
 

@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
             const double pzp = pr[n + sz], pzm = pr[n - sz];
             r = q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
                      typ * (pyp - p0) + tzp * (pzp - p0));
-            if (want_b) {
+            if (want_b && (q != 0.0 || ((fl[n - sz] | fl[n - sy] | fl[n - 1] | fl[n + 1] |
+                                         fl[n + sy] | fl[n + sz]) & F_DIR))) {
                 double bref = -q;
                 if (fl[n - sz] & F_DIR) bref -= pzm * tzm;
                 if (fl[n - sy] & F_DIR) bref -= pym * tym;
@@ -151,14 +152,20 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
             const double pzp = pr[n + sz], pzm = pr[n - sz];
             r0 = q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
                       typ * (pyp - p0) + tzp * (pzp - p0));
-            double bref = -q;
-            if (fl[n - sz] & F_DIR) bref -= pzm * tzm;
-            if (fl[n - sy] & F_DIR) bref -= pym * tym;
-            if (fl[n - 1] & F_DIR) bref -= pxm * txm;
-            if (fl[n + 1] & F_DIR) bref -= pxp * txp;
-            if (fl[n + sy] & F_DIR) bref -= pyp * typ;
-            if (fl[n + sz] & F_DIR) bref -= pzp * tzp;
-            bb += bref * bref;
+            // b_ref differs from -q only next to a Dirichlet cell: branch on
+            // the neighbour flags so that interior cells issue no FP64 there
+            const uint8_t dm = (fl[n - sz] | fl[n - sy] | fl[n - 1] | fl[n + 1] | fl[n + sy] |
+                                fl[n + sz]) & F_DIR;
+            if (dm || q != 0.0) {
+                double bref = -q;
+                if (fl[n - sz] & F_DIR) bref -= pzm * tzm;
+                if (fl[n - sy] & F_DIR) bref -= pym * tym;
+                if (fl[n - 1] & F_DIR) bref -= pxm * txm;
+                if (fl[n + 1] & F_DIR) bref -= pxp * txp;
+                if (fl[n + sy] & F_DIR) bref -= pyp * typ;
+                if (fl[n + sz] & F_DIR) bref -= pzp * tzp;
+                bb += bref * bref;
+            }
             e = ws_ext(d1, d2, a, b, n);
             const R ae = diag[n] * (R)e -
                          (cx[n] * (R)ws_ext(d1, d2, a, b, n + 1) + cx[n - 1] * (R)ws_ext(d1, d2, a, b, n - 1) +
