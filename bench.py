@@ -62,6 +62,8 @@ def parse():
                     help="launch the preconditioner cycle kernel by kernel")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 MG-PCG comparison run")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the run with the learned correction of the start")
     ap.add_argument("--spinup", type=int, default=40,
                     help="untimed steps before the warm-up: the timed window starts past "
                          "the start-up transient of the run (dt jump at step 3, first front "
@@ -292,6 +294,7 @@ def run_ours(args):
         "fused_update_ms": upd_ms,
         "fused_update_gbs": upd_bytes / (upd_ms / 1000.0) / 1e9 if upd_ms > 0 else None,
         "gpu_launches": int(n1.value - n0.value),
+        "launches_before_timed": int(n0.value),   # skip count for a launch list of the timed steps
         "roofline": roof,
         "clocks": clk,
         "kernel_class_ms": ({KC_NAMES[c]: float(kms[c]) / args.steps for c in range(NK)}
@@ -305,6 +308,8 @@ def run_ours(args):
     if args.solver == "mixed" and not args.no_plain:
         out["plain_fp64"] = plain_fp64_pass(args, case, world)
         out["speedup_vs_plain_fp64"] = value / out["plain_fp64"]["value"]
+    if args.solver == "mixed" and not args.no_learned:
+        out["learned"] = learned_pass(args, case, world)
     if not args.no_e2e:
         out["e2e"] = e2e_pass(args, sim, stream, world)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -317,6 +322,53 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def learned_pass(args, case, world):
+    """The same run with the learned correction on top of the extrapolated
+    start (weights trained on 128^3 runs, mizuho_edit_gb300/weights), timed
+    the same way; reports what it changes against the headline run."""
+    import torch
+    from mizuho_edit_gb300 import capi, learned
+    from mizuho_edit_gb300.sim import Simulation
+    path = learned.DEFAULT_WEIGHTS
+    if not os.path.exists(path):
+        return {"unavailable": "no trained weights at mizuho_edit_gb300/weights"}
+    n = args.n
+    net = learned.WarmStartNet(n // 2, n // 2, n // 2)
+    net.set_params(learned.WarmStartNet.load_params(path))
+    kw = solver_kwargs(args)
+    kw["extrapolate"] = True
+    with Simulation(case.params, case.permeab_rock, case.phase, case.concent, **kw) as sim:
+        learned.attach(sim, net)
+        for _ in range(args.spinup + args.warmup):
+            sim.step()
+        sp = C.c_void_p()
+        capi.check(sim.L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
+        stream = torch.cuda.ExternalStream(sp.value)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        stats = [sim.step() for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = torch.tensor([e0.elapsed_time(e1)], device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        learned.attach(sim, None)
+    net.close()
+    return {"value": world * args.steps / (ms / 1000.0), "unit": "time-steps/s",
+            "ms_per_step": ms / args.steps,
+            "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
+            "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
+            "relres0_mean": statistics.mean(s.relres0 for s in stats),
+            "net_start_kept": sum(1 for s in stats if s.warm_start == 2),
+            "extrapolation_only": sum(1 for s in stats if s.warm_start == 1),
+            "fallbacks_to_previous_pressure": sum(1 for s in stats if s.warm_start == -1),
+            "relres_max": max(s.relres for s in stats)}
 
 
 def plain_fp64_pass(args, case, world):

@@ -125,6 +125,10 @@ typedef struct wpf_diag {
     double phase_max, phase_min, concent_max, concent_min;   /* over G incl. halo      */
     double pressure_ref;       /* getPressure(ix_ref, iy_ref, iz_ref) (:2151-2166)      */
     double inlet_flux;         /* sum of u_x across the faces ix = 1 | 2, times dx^2    */
+    double phase_max_outlet;   /* max phase over the cells ix = nx-1: breakthrough when
+                                  > 0 (no counterpart in the reference, whose
+                                  showProgress cannot report it under Dirichlet BCs);
+                                  NaN from wpf_reduce_noalloc                          */
 } wpf_diag;
 
 /* ---- lifetime ------------------------------------------------------------
@@ -221,6 +225,18 @@ int wpf_kernel_times(wpf_handle* h, double* ms, int64_t* counts, int32_t n);
  * copies in wpf_upload / wpf_download then run at full link bandwidth).     */
 int wpf_host_alloc(int64_t bytes, void** ptr);
 int wpf_host_free(void* ptr);
+
+/* Asynchronous single-precision snapshot of the four fields saveResult writes
+ * (wPFAW3D.f90:1934-2037: pressure, phase, concentration and the cell
+ * permeability permeab(0) of the phase the last step started from), for a
+ * GiD result writer.  `out` (page-locked, 4 * nx*ny*nz floats) receives them
+ * one after the other, interior cells in Fortran order, converted like the
+ * reference's real(x, kind=4).  The call packs the fields on the device and
+ * queues the copy on a side stream, then returns: the simulation can go on
+ * stepping while the copy runs.  wpf_snapshot_wait blocks until the last
+ * snapshot has landed in `out`.                                            */
+int wpf_snapshot(wpf_handle* h, float* out);
+int wpf_snapshot_wait(wpf_handle* h);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ LIB_NAME = "libwpf_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["wpf_capi.cu", "wpf_physics.cu", "wpf_solver.cu", "wpf_noalloc.cu"]
+SOURCES = ["wpf_capi.cu", "wpf_physics.cu", "wpf_solver.cu", "wpf_noalloc.cu", "wpf_net.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
@@ -47,6 +47,7 @@ def up_to_date() -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
+        build_driver()
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     cc = nvcc()
@@ -69,7 +70,28 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
+    build_driver()
     return LIB_PATH
+
+
+DRIVER_SRC = os.path.join(HERE, "host", "wpf_driver.cpp")
+DRIVER_PATH = os.path.join(BUILD_DIR, "wpf_driver")
+
+
+def build_driver() -> str:
+    """The C++ host program (program main of the reference) on the C ABI."""
+    if (os.path.exists(DRIVER_PATH) and os.path.getmtime(DRIVER_PATH) >= os.path.getmtime(DRIVER_SRC)
+            and os.path.getmtime(DRIVER_PATH) >= os.path.getmtime(LIB_PATH)):
+        return DRIVER_PATH
+    cxx = shutil.which("g++") or "g++"
+    tmp = DRIVER_PATH + f".tmp{os.getpid()}"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, DRIVER_SRC, "-L", BUILD_DIR, "-lwpf_gb300",
+           "-Wl,-rpath,$ORIGIN", "-pthread", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER_PATH)
+    return DRIVER_PATH
 
 
 if __name__ == "__main__":

@@ -71,7 +71,8 @@ class Diag(C.Structure):
     _fields_ = [("pv", C.c_double), ("vcal", C.c_double), ("rwhmax", C.c_double),
                 ("phase_max", C.c_double), ("phase_min", C.c_double),
                 ("concent_max", C.c_double), ("concent_min", C.c_double),
-                ("pressure_ref", C.c_double), ("inlet_flux", C.c_double)]
+                ("pressure_ref", C.c_double), ("inlet_flux", C.c_double),
+                ("phase_max_outlet", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -110,6 +111,27 @@ SIGNATURES = {
     "wpf_kernel_times": (C.c_int, [H, DP, C.POINTER(C.c_int64), C.c_int32]),
     "wpf_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
     "wpf_host_free": (C.c_int, [C.c_void_p]),
+    "wpf_snapshot": (C.c_int, [H, C.c_void_p]),
+    "wpf_snapshot_wait": (C.c_int, [H]),
+    # include/wpf_net.h: the learned warm start
+    "wpf_net_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "wpf_net_destroy": (C.c_int, [C.c_void_p]),
+    "wpf_net_init": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "wpf_net_param_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "wpf_net_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wpf_net_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wpf_net_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "wpf_net_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                     C.POINTER(C.c_float), C.c_void_p]),
+    "wpf_net_get_grads": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wpf_net_get_activation": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "wpf_conv3d": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                             C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "wpf_conv3d_wgrad": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "wpf_set_warm_start_net": (C.c_int, [H, C.c_void_p]),
+    "wpf_ws_features": (C.c_int, [H, C.c_double, C.c_void_p]),
+    "wpf_ws_target": (C.c_int, [H, C.c_void_p]),
 }
 
 _lib = None

@@ -244,6 +244,113 @@ def load_config(path: str, extended: bool = True) -> Params:
     return p
 
 
+def load_input(path: str) -> Params:
+    """Parse a legacy ``.inp`` file as ``loadInput`` does (wPFAW3D.f90:110-259):
+    a fixed sequence of comment records and list-directed reads (a read that
+    finds too few values on its record continues on the next ones), the wells
+    inline, then the uniform initial K, phase and concentration."""
+    try:
+        with open(path, "r") as fh:
+            lines = fh.read().splitlines()
+    except OSError as e:
+        raise ConfigError(f"can not open input file: {path}") from e
+    pos = 0
+
+    def skip(n):
+        nonlocal pos
+        pos += n
+
+    def read(n):
+        nonlocal pos
+        out = []
+        while len(out) < n:
+            if pos >= len(lines):
+                raise ConfigError(f"invalid data in input file: {path}")
+            out += _split(lines[pos])
+            pos += 1
+        return out[:n]
+
+    p = Params()
+    try:
+        skip(5)
+        p.nx, p.ny, p.nz = (_int(t) for t in read(3))
+        skip(1)
+        a = read(2)
+        p.dtime, p.tfac = _num(a[0]), _num(a[1])
+        skip(1)
+        a = read(4)
+        p.time_start, p.time_end = _num(a[0]), _num(a[1])
+        p.n_res_out, p.n_dat_out = _int(a[2]), _int(a[3])
+        skip(2)
+        a = read(2)
+        p.epsilon, dxw = _num(a[0]), _num(a[1])
+        skip(1)
+        p.lambda_ = _num(read(1)[0])
+        skip(2)
+        p.porosity = _num(read(1)[0])
+        skip(1)
+        p.rhos, p.rhoa = (_num(t) for t in read(2))
+        skip(1)
+        p.viscosity = _num(read(1)[0])
+        skip(1)
+        p.cwtp = _num(read(1)[0])
+        skip(1)
+        p.diffusion = _num(read(1)[0])
+        skip(2)
+        p.b100 = _num(read(1)[0])
+        skip(1)
+        p.ral, p.rat = (_num(t) for t in read(2))
+        skip(1)
+        p.permeab_hole = _num(read(1)[0])
+        skip(1)
+        p.pini = _num(read(1)[0])
+        skip(1)
+        p.ix_ref, p.iy_ref, p.iz_ref = (_int(t) for t in read(3))
+        skip(2)
+        for _ in range(_int(read(1)[0])):
+            t = read(7)
+            ix, iy, iz, wpq = (_int(x) for x in t[:4])
+            wval, ph, c = (_num(x) for x in t[4:7])
+            if wpq == 1:
+                p.wells.append(Well(ix, iy, iz, pressure=wval, injection=0.0, phase=ph, concent=c))
+            elif wpq == -1:
+                p.wells.append(Well(ix, iy, iz, pressure=0.0, injection=wval, phase=ph, concent=c))
+            else:
+                raise ConfigError(f"invalid well data in input file: {path}")
+        skip(2)
+        p.init_permeab = _num(read(1)[0])
+        skip(1)
+        p.init_phase = _num(read(1)[0])
+        skip(1)
+        p.init_concent = _num(read(1)[0])
+    except (IndexError, ValueError) as e:
+        raise ConfigError(f"invalid data in input file: {path}") from e
+    p.time_total = p.time_end - p.time_start
+    p.dxw = dxw
+    derive(p)
+    return p
+
+
+def write_input(path: str, p: Params) -> None:
+    """A legacy ``.inp`` file that load_input / loadInput read back as ``p``."""
+    L = ["# wPFAW3D input", "#", "#", "#", "# grid nx ny nz", f"{p.nx} {p.ny} {p.nz}",
+         "# dt tfac", f"{p.dtime!r} {p.tfac!r}",
+         "# time_start time_end n_res n_dat", f"{p.time_start!r} {p.time_end!r} {p.n_res_out} {p.n_dat_out}",
+         "# phase field", "# w dxw", f"{p.epsilon!r} {p.dxw!r}", "# lambda", f"{p.lambda_!r}",
+         "# rock and fluid", "# poro", f"{p.porosity!r}", "# rhos rhoa", f"{p.rhos!r} {p.rhoa!r}",
+         "# visco", f"{p.viscosity!r}", "# cwtp", f"{p.cwtp!r}", "# D", f"{p.diffusion!r}",
+         "# reaction", "# b100", f"{p.b100!r}", "# ral rat", f"{p.ral!r} {p.rat!r}",
+         "# kwh", f"{p.permeab_hole!r}", "# pini", f"{p.pini!r}", "# ref", f"{p.ix_ref} {p.iy_ref} {p.iz_ref}",
+         "# wells", "# nwell", f"{len(p.wells)}"]
+    for w in p.wells:
+        wpq, wval = (1, w.pressure) if (w.pressure != 0.0 or w.injection == 0.0) else (-1, w.injection)
+        L.append(f"{w.ix} {w.iy} {w.iz} {wpq} {wval!r} {w.phase!r} {w.concent!r}")
+    L += ["# initial fields", "# K", f"{p.init_permeab!r}", "# phase", f"{p.init_phase!r}", "# concent",
+          f"{p.init_concent!r}"]
+    with open(path, "w") as fh:
+        fh.write("\n".join(L) + "\n")
+
+
 def write_well_file(path: str, wells: Sequence[Well]) -> None:
     with open(path, "w") as fh:
         fh.write("# ix iy iz wpq wval phase concent\n")

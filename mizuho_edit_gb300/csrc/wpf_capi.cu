@@ -124,6 +124,10 @@ static void free_all(wpf_handle* h) {
         if (p) cudaFree(p);
     if (h->flags) cudaFree(h->flags);
     if (h->work) cudaFree(h->work);
+    if (h->snap) cudaFree(h->snap);
+    if (h->snap_ready) cudaEventDestroy(h->snap_ready);
+    if (h->snap_done) cudaEventDestroy(h->snap_done);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->dphys) cudaFree(h->dphys);
     if (h->dir_idx) cudaFree(h->dir_idx);
     solver_free(h);
@@ -323,6 +327,25 @@ __global__ void k_repitch(Grid g, const double* __restrict__ src, double* __rest
     }
 }
 
+// FP32 dense interior copies of pressure, phase, concentration and the cell
+// permeability K0 = kwh f + Krock (1 - f), f = (1 + phase)/2 (:567-574) of kph.
+__global__ void __launch_bounds__(RB) k_snapshot(Grid g, Phys P, const double* __restrict__ pr,
+                                                 const double* __restrict__ ph,
+                                                 const double* __restrict__ cc,
+                                                 const double* __restrict__ kph,
+                                                 const double* __restrict__ kr, float* __restrict__ out) {
+    const long long N = (long long)g.nx * g.ny * g.nz;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        const long long d = (i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
+        const double f = 0.5 * (1.0 + kph[n]);
+        out[d] = (float)pr[n];
+        out[N + d] = (float)ph[n];
+        out[2 * N + d] = (float)cc[n];
+        out[3 * N + d] = (float)(P.kwh * f + kr[n] * (1.0 - f));
+    }
+}
+
 static int ensure_staging(wpf_handle* h) {
     if (h->staging) return WPF_OK;
     const Grid& g = h->g;
@@ -365,6 +388,7 @@ int wpf_upload(wpf_handle* h, const double* krock, const double* phase, const do
         if ((rc = phys_set_dirichlet(h))) return rc;
     }
     h->vel_valid = false;
+    if (krock) h->ws_klog_ready = false;   // the learned start's input statistics change
     if (phase || krock) {
         h->kf_valid = false;
         h->t_current = false;
@@ -558,6 +582,39 @@ int wpf_host_alloc(int64_t bytes, void** ptr) {
         *ptr = nullptr;
         return WPF_ERR_NOMEM;
     }
+    return WPF_OK;
+}
+
+int wpf_snapshot(wpf_handle* h, float* out) {
+    if (!h || !out) return WPF_ERR_ARG;
+    const Grid& g = h->g;
+    const long long N = (long long)g.nx * g.ny * g.nz;
+    if (!h->snap) {
+        int rc = dev_alloc(h, (void**)&h->snap, sizeof(float) * 4 * N);
+        if (rc) return rc;
+        WPF_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->snap_ready, cudaEventDisableTiming));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->snap_done, cudaEventDisableTiming));
+    }
+    // the staging buffer is reused: the previous copy must have left it
+    if (h->snap_pending) WPF_CUDA(cudaStreamWaitEvent(h->stream, h->snap_done, 0));
+    // K0 of the phase the last fused step started from (phase_n after it)
+    const double* kph = h->t_from_prev ? h->phase_n : h->phase;
+    WPF_LAUNCH(h, KC_OTHER, k_snapshot<<<row_blocks(h, g), RB, 0, h->stream>>>(
+        g, h->phys, h->pressure, h->phase, h->concent, kph, h->krock, h->snap));
+    WPF_CUDA(cudaGetLastError());
+    WPF_CUDA(cudaEventRecord(h->snap_ready, h->stream));
+    WPF_CUDA(cudaStreamWaitEvent(h->side, h->snap_ready, 0));
+    WPF_CUDA(cudaMemcpyAsync(out, h->snap, sizeof(float) * 4 * N, cudaMemcpyDeviceToHost, h->side));
+    WPF_CUDA(cudaEventRecord(h->snap_done, h->side));
+    h->snap_pending = true;
+    return WPF_OK;
+}
+
+int wpf_snapshot_wait(wpf_handle* h) {
+    if (!h) return WPF_ERR_ARG;
+    if (h->snap_pending) WPF_CUDA(cudaEventSynchronize(h->snap_done));
+    h->snap_pending = false;
     return WPF_OK;
 }
 

@@ -52,6 +52,7 @@ enum Slot {
     S_RR64,             // ||r||^2 of the FP64 residual
     S_BB64,             // ||b||^2 of the reference right-hand side
     S_RR0WS,            // ||r(p)||^2 when the solve tries an extrapolated start
+    S_RW, S_WW,         // r_ext . A'e_net and ||A'e_net||^2 (step length of the learned start)
     S_PQ,               // PCG p.q
     S_RR,               // PCG r.r
     S_RZ0, S_RZ1,       // PCG r.z (double buffered)
@@ -59,6 +60,10 @@ enum Slot {
     S_MAX0, S_MAX1, S_MAX2, S_MAX3, S_MAX4,
     S_NWORK,            // work-list counts of the fused update: interface cells and
                         // concentration-only cells (two ints in a double slot)
+    S_WSS2,             // sum of the squared last increment (input scale of the learned start)
+    S_WSD2,             // sum of the squared change of the increment (its output scale)
+    S_DPH2,             // sum of the squared phase change of the last step (its scale)
+    S_KLOG0, S_KLOG1,   // sum of log K_rock and of its square (input normalisation)
     S_COUNT = 32
 };
 
@@ -138,6 +143,16 @@ struct wpf_handle {
     double ws_hn, ws_h1, ws_h2;   // step sizes: this step, previous, one before (0 = unknown)
     long long ws_fallbacks;  // solves whose extrapolated start was rejected
     double* staging;         // dense halo-array staging for host copies (lazily allocated)
+    struct wpf_net* ws_net;  // learned warm start (not owned), or null
+    float* ws_e[2];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output)
+    uint16_t* ws_in;         // net input (bf16, net grid, 16 channels)
+    float* ws_out;           // net output channel 0 (net grid)
+    bool ws_klog_ready;      // S_KLOG0/1 hold the statistics of log K_rock
+    // asynchronous output snapshots: FP32 device staging, side stream, events
+    float* snap;
+    cudaStream_t side;
+    cudaEvent_t snap_ready, snap_done;
+    bool snap_pending;
     double* dsc;             // device scalar slots
     double* hsc;             // pinned host mirror of the scalar slots
     double* partials;        // per-block partial sums of the diagnostics
@@ -350,6 +365,10 @@ int solver_setup(wpf_handle* h);
 int solver_free(wpf_handle* h);
 void solver_drop_graphs(wpf_handle* h);   // after an options change
 int solve_pressure(wpf_handle* h, wpf_step_stats* st);
+// extrapolated / learned start (wpf_solver.cu, wpf_net.cu)
+void ws_coeffs(const wpf_handle* h, float* a, float* b);
+int ws_build_ext(wpf_handle* h, float a, float b);      // ws_e[0] = a d1 + b d2, S_WSS2 = sum d1^2
+int ws_net_correction(wpf_handle* h);                   // ws_e[1] from the attached net
 
 int ensure_per_routine_arrays(wpf_handle* h);
 int dev_alloc(wpf_handle* h, void** p, size_t bytes);

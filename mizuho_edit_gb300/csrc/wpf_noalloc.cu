@@ -151,5 +151,6 @@ extern "C" int wpf_reduce_noalloc(const wpf_params* p, const double* d_phase,
     out->concent_min = r[6];
     out->pressure_ref = 0.0;
     out->inlet_flux = 0.0;
+    out->phase_max_outlet = NAN;   // not reduced here (like the two above)
     return WPF_OK;
 }

@@ -107,19 +107,42 @@ __global__ void __launch_bounds__(RB) k_add_correction(Grid g, double* __restric
     }
 }
 
-// ---- extrapolated warm start ------------------------------------------------
-// e = a d1 + b d2 from the last two increments, rounded the same way in every
-// kernel that forms it.
-__device__ __forceinline__ float ws_ext(const float* __restrict__ d1, const float* __restrict__ d2,
-                                        float a, float b, long long n) {
-    return __fmaf_rn(a, d1[n], __fmul_rn(b, d2[n]));
+// ---- extrapolated / learned warm start ------------------------------------------
+// e_ext = a d1 + b d2 from the last two increments (zero on Dirichlet cells,
+// where every increment is zero); accumulates sum d1^2 and sum (d1 - d2)^2
+// (the scales the learned start works in) into S_WSS2 and S_WSD2.
+__global__ void __launch_bounds__(RB) k_ws_build_ext(Grid g, const float* __restrict__ d1,
+                                                     const float* __restrict__ d2, float a, float b,
+                                                     float* __restrict__ e, double* dsc) {
+    double s2 = 0.0, q2 = 0.0;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        const float v1 = d1[n], v2 = d2[n];
+        e[n] = __fmaf_rn(a, v1, __fmul_rn(b, v2));
+        s2 += (double)v1 * v1;
+        const double dd = (double)v1 - (double)v2;
+        q2 += dd * dd;
+    }
+    block_add(s2, dsc + S_WSS2);
+    block_add(q2, dsc + S_WSD2);
 }
 
-// Pass-0 residual of the start p + e: r0 = r(p) in FP64 exactly as
+template <typename R>
+__device__ __forceinline__ R apply_l0(const R* __restrict__ cx, const R* __restrict__ cy,
+                                      const R* __restrict__ cz, const R* __restrict__ diag,
+                                      const float* __restrict__ e, long long n, long long sy, long long sz) {
+    return diag[n] * (R)e[n] - (cx[n] * (R)e[n + 1] + cx[n - 1] * (R)e[n - 1] + cy[n] * (R)e[n + sy] +
+                                cy[n - sy] * (R)e[n - sy] + cz[n] * (R)e[n + sz] + cz[n - sz] * (R)e[n - sz]);
+}
+
+// Pass-0 residual of the start p + e_ext: r0 = r(p) in FP64 exactly as
 // k_resid64 (||r0||^2 into S_RR0WS, ||b_ref||^2 into S_BB64), then
-// r1 = r0 - A'e with A'e from the level-0 coefficients in precision R (e is a
-// small increment, so its rounding stays orders of magnitude below the outer
-// tolerance); writes r1 and dnew = e, accumulates ||r1||^2 into S_RR64.
+// r_ext = r0 - A'e_ext with A'e from the level-0 coefficients in precision R
+// (e is a small increment, so its rounding stays orders of magnitude below the
+// outer tolerance); writes rout = r_ext, dnew = e_ext, ||r_ext||^2 into S_RR64.
+// With a learned correction e_net: also w = A'e_net, r_ext.w into S_RW and
+// w.w into S_WW, from which the host takes the step alpha = r.w / w.w that
+// minimises ||r_ext - alpha w|| (so the correction never raises the residual).
 template <typename R>
 __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restrict__ pr,
                                                    const double* __restrict__ Tx,
@@ -130,11 +153,11 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    const R* __restrict__ cx, const R* __restrict__ cy,
                                                    const R* __restrict__ cz,
                                                    const R* __restrict__ diag,
-                                                   const float* __restrict__ d1,
-                                                   const float* __restrict__ d2, float a, float b,
+                                                   const float* __restrict__ e1,
+                                                   const float* __restrict__ e2,
                                                    R* __restrict__ rout, float* __restrict__ dnew,
                                                    double* dsc) {
-    double rr1 = 0.0, rr0 = 0.0, bb = 0.0;
+    double rr1 = 0.0, rr0 = 0.0, bb = 0.0, rw = 0.0, ww = 0.0;
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
@@ -166,12 +189,13 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                 if (fl[n + sz] & F_DIR) bref -= pzp * tzp;
                 bb += bref * bref;
             }
-            e = ws_ext(d1, d2, a, b, n);
-            const R ae = diag[n] * (R)e -
-                         (cx[n] * (R)ws_ext(d1, d2, a, b, n + 1) + cx[n - 1] * (R)ws_ext(d1, d2, a, b, n - 1) +
-                          cy[n] * (R)ws_ext(d1, d2, a, b, n + sy) + cy[n - sy] * (R)ws_ext(d1, d2, a, b, n - sy) +
-                          cz[n] * (R)ws_ext(d1, d2, a, b, n + sz) + cz[n - sz] * (R)ws_ext(d1, d2, a, b, n - sz));
-            r1 = r0 - (double)ae;
+            e = e1[n];
+            r1 = r0 - (double)apply_l0(cx, cy, cz, diag, e1, n, sy, sz);
+            if (e2) {
+                const double w = (double)apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+                rw += r1 * w;
+                ww += w * w;
+            }
         }
         rout[n] = (R)r1;
         dnew[n] = e;
@@ -181,22 +205,41 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
     block_add(rr1, dsc + S_RR64);
     block_add(rr0, dsc + S_RR0WS);
     block_add(bb, dsc + S_BB64);
+    if (e2) {
+        block_add(rw, dsc + S_RW);
+        block_add(ww, dsc + S_WW);
+    }
 }
 
-// p += e (add_ext: the extrapolated start, added once) + x (the pass's
-// correction, when x != null); dnew accumulates x, so that after the last
-// pass it holds this solve's whole increment.
+// Accept the learned correction with step alpha: r -= alpha A'e_net,
+// dnew += alpha e_net.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_ws_take_net(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
+                                                    const R* __restrict__ cz, const R* __restrict__ diag,
+                                                    const uint8_t* __restrict__ fl, float alpha,
+                                                    const float* __restrict__ e2, R* __restrict__ r,
+                                                    float* __restrict__ dnew) {
+    const long long sy = g.P, sz = g.S;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        dnew[n] += alpha * e2[n];
+        if (!(fl[n] & F_DIR)) r[n] -= (R)alpha * apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+    }
+}
+
+// p += e (e1 [+ alpha e2]: the accepted start, added once, when e1 != null)
+// + x (the pass's correction, when x != null); dnew accumulates x, so that
+// after the last pass it holds this solve's whole increment.
 template <typename R>
 __global__ void __launch_bounds__(RB) k_add_correction_ws(Grid g, double* __restrict__ pr,
                                                           const R* __restrict__ x,
-                                                          const float* __restrict__ d1,
-                                                          const float* __restrict__ d2, float a,
-                                                          float b, int add_ext,
+                                                          const float* __restrict__ e1,
+                                                          const float* __restrict__ e2, float alpha,
                                                           float* __restrict__ dnew) {
     ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         double inc = x ? (double)x[n] : 0.0;
-        if (add_ext) inc += (double)ws_ext(d1, d2, a, b, n);
+        if (e1) inc += (double)(e2 ? e1[n] + alpha * e2[n] : e1[n]);
         pr[n] += inc;
         if (x) dnew[n] += (float)x[n];
     }
@@ -1166,6 +1209,14 @@ int solver_free(wpf_handle* h) {
         if (h->ws[q]) cudaFree(h->ws[q]);
         h->ws[q] = nullptr;
     }
+    for (int q = 0; q < 2; ++q) {
+        if (h->ws_e[q]) cudaFree(h->ws_e[q]);
+        h->ws_e[q] = nullptr;
+    }
+    if (h->ws_in) cudaFree(h->ws_in);
+    if (h->ws_out) cudaFree(h->ws_out);
+    h->ws_in = nullptr;
+    h->ws_out = nullptr;
     h->ws_hist = 0;
     return WPF_OK;
 }
@@ -1175,7 +1226,7 @@ int solver_free(wpf_handle* h) {
 //   e = (hn/h1) d1 + hn (hn + h1) / (h1 + h2) (d1/h1 - d2/h2),
 // (linear, e = (hn/h1) d1, with one increment; equal steps when a step size
 // is unknown: 2 d1 - d2, d1).
-static void ws_coeffs(const wpf_handle* h, float* a, float* b) {
+void ws_coeffs(const wpf_handle* h, float* a, float* b) {
     *a = 0.f;
     *b = 0.f;
     if (h->ws_hist <= 0) return;
@@ -1194,6 +1245,19 @@ static void ws_coeffs(const wpf_handle* h, float* a, float* b) {
     *b = (float)(-c / h2);
 }
 
+int ws_build_ext(wpf_handle* h, float a, float b) {
+    const Grid& g = h->g;
+    if (!h->ws_e[0]) {
+        int rc = dev_alloc(h, (void**)&h->ws_e[0], sizeof(float) * g.total);
+        if (rc) return rc;
+    }
+    WPF_CUDA(cudaMemsetAsync(h->dsc + S_WSS2, 0, 2 * sizeof(double), h->stream));   // WSS2, WSD2
+    WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<row_blocks(h, g), RB, 0, h->stream>>>(
+        g, h->ws[0], h->ws[1], a, b, h->ws_e[0], h->dsc));
+    WPF_CUDA(cudaGetLastError());
+    return WPF_OK;
+}
+
 template <typename R>
 static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     const Grid& g = h->g;
@@ -1205,33 +1269,55 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     const int nu = h->opts.smooth_sweeps > 0 ? h->opts.smooth_sweeps : 2;
     int outer = 0, inner_total = 0, status = WPF_ERR_NOT_CONVERGED;
     double relres = 0.0, bnorm = 0.0, relres0 = 0.0;
-    // extrapolated start: tried on pass 0 when two (or one) increments are held
+    // extrapolated start: tried on pass 0 when two (or one) increments are
+    // held; with an attached net, the net's correction on top of it too
     const bool ws_on = (h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && h->ws[0];
-    float wa = 0.f, wb = 0.f;
-    if (ws_on) ws_coeffs(h, &wa, &wb);
-    float *d1 = ws_on ? h->ws[0] : nullptr, *d2 = ws_on ? h->ws[1] : nullptr;
     float* dnew = ws_on ? h->ws[2] : nullptr;
-    bool ext_pending = false;   // e accepted but not yet added to the pressure
+    const float* e1 = nullptr;   // the accepted start (added to p once): e_ext ...
+    const float* e2 = nullptr;   // ... + alpha e_net
+    float alpha = 0.f;
+    bool ext_pending = false;    // a start accepted but not yet added to the pressure
     h->ws_used = 0;
     for (int pass = 0; pass <= h->opts.max_outer; ++pass) {
-        WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 3 * sizeof(double), s));   // RR64, BB64, RR0WS
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 5 * sizeof(double), s));   // RR64 BB64 RR0WS RW WW
         bool plain = true;
         if (pass == 0 && ws_on && h->ws_hist > 0) {
+            float wa = 0.f, wb = 0.f;
+            ws_coeffs(h, &wa, &wb);
+            if ((rc = ws_build_ext(h, wa, wb))) return rc;
+            const bool net = h->ws_net && h->ws_hist >= 2;
+            if (net && (rc = ws_net_correction(h))) return rc;
             WPF_LAUNCH(h, KC_RESID64, k_resid64_ws<R><<<rb, RB, 0, s>>>(
                 g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, H.lv[0].cx, H.lv[0].cy,
-                H.lv[0].cz, H.lv[0].diag, d1, d2, wa, wb, H.r, dnew, h->dsc));
+                H.lv[0].cz, H.lv[0].diag, h->ws_e[0], net ? h->ws_e[1] : nullptr, H.r, dnew, h->dsc));
             WPF_CUDA(cudaGetLastError());
-            rc = read_slot(h, S_RR64, 3);
+            rc = read_slot(h, S_RR64, 5);
             if (rc) return rc;
-            const double r1 = h->hsc[S_RR64], r0 = h->hsc[S_RR0WS];
-            if (r1 <= r0 && r1 == r1) {   // the fallback rule: keep p + e only if it is better
+            double rstart = h->hsc[S_RR64];
+            const double r0 = h->hsc[S_RR0WS], rw = h->hsc[S_RW], ww = h->hsc[S_WW];
+            // learned correction: the step that minimises the residual along it
+            if (net && ww > 0.0 && rw > 0.0 && rw == rw) {
+                alpha = (float)(rw / ww);
+                rstart = fmax(rstart - rw * rw / ww, 0.0);
+            }
+            // the fallback rule: the start is kept only when its FP64-evaluated
+            // residual is below that of p itself (the reference's start)
+            if (rstart <= r0 && rstart == rstart) {
                 plain = false;
                 ext_pending = true;
+                e1 = h->ws_e[0];
                 h->ws_used = 1;
+                if (alpha > 0.f) {
+                    e2 = h->ws_e[1];
+                    h->ws_used = 2;
+                    WPF_LAUNCH(h, KC_RESID64, k_ws_take_net<R><<<rb, RB, 0, s>>>(
+                        g, H.lv[0].cx, H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->flags, alpha, e2, H.r, dnew));
+                }
+                h->hsc[S_RR64] = rstart;
             } else {
                 h->ws_used = -1;
                 ++h->ws_fallbacks;
-                WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 3 * sizeof(double), s));
+                WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 5 * sizeof(double), s));
             }
         }
         if (plain) {
@@ -1252,7 +1338,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             // already meets rtol is added to p and verified by a plain FP64 pass
             if (ext_pending && pass < h->opts.max_outer) {
                 WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(
-                    g, h->pressure, (const R*)nullptr, d1, d2, wa, wb, 1, dnew));
+                    g, h->pressure, (const R*)nullptr, e1, e2, alpha, dnew));
                 ext_pending = false;
                 continue;
             }
@@ -1269,8 +1355,8 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         inner_total += its;
         if (rc == WPF_ERR_NONFINITE) { status = rc; break; }
         if (ws_on)
-            WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x, d1, d2, wa,
-                                                                           wb, ext_pending, dnew));
+            WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(
+                g, h->pressure, H.x, ext_pending ? e1 : nullptr, e2, alpha, dnew));
         else
             WPF_LAUNCH(h, KC_VEC, k_add_correction<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x));
         ext_pending = false;
@@ -1278,7 +1364,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     }
     if (ext_pending)   // max_outer = 0: the start was accepted but never verified
         WPF_LAUNCH(h, KC_VEC, k_add_correction_ws<R><<<rb, RB, 0, s>>>(g, h->pressure, (const R*)nullptr,
-                                                                       d1, d2, wa, wb, 1, dnew));
+                                                                       e1, e2, alpha, dnew));
     if (ws_on) {
         if (status == WPF_OK) {   // this increment becomes the newest of the history
             float* t = h->ws[1];

@@ -1,0 +1,203 @@
+"""Learned warm start of the Darcy solve: data generation, training, evaluation.
+
+The network (include/wpf_net.h, kernels in csrc/wpf_net.cu) maps the state at
+half resolution -- log K_rock, phase, pressure, the last two pressure
+increments, their time extrapolation and the phase change of the last step --
+to a correction of the extrapolated increment.  Its training data are pairs
+(input, target) that the simulator itself produces: target = (the solve's
+increment - the extrapolation), restricted 2x2x2 and scaled by the rms of the
+last increment.  The solve always finishes at the same FP64 residual
+tolerance and keeps the network's start only when its FP64 residual is the
+smallest of the candidates (previous pressure, extrapolation, extrapolation +
+network), so the network changes iteration counts, never the answer.
+
+PyTorch only holds device memory here; every kernel is the library's.
+
+    python -m mizuho_edit_gb300.learned train --out weights.npz [--runs 20 --n 128 ...]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import time
+
+import numpy as np
+
+from . import capi
+from .cases import make_case
+from .sim import Simulation
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "warm_start_unet.npz")
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class WarmStartNet:
+    """One wpf_net for an (nx, ny, nz) net grid (half the simulation grid)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, seed: int = 0):
+        self.L = capi.load()
+        h = C.c_void_p()
+        capi.check(self.L.wpf_net_create(nx, ny, nz, C.byref(h)), "wpf_net_create")
+        self.h = h
+        self.dims = (nx, ny, nz)
+        capi.check(self.L.wpf_net_init(h, seed), "wpf_net_init")
+        n = C.c_int64()
+        self.L.wpf_net_param_count(h, C.byref(n))
+        self.nparam = n.value
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparam, np.float32)
+        capi.check(self.L.wpf_net_get_params(self.h, out.ctypes.data_as(C.c_void_p)), "get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.nparam:
+            raise ValueError(f"expected {self.nparam} parameters, got {p.size}")
+        capi.check(self.L.wpf_net_set_params(self.h, p.ctypes.data_as(C.c_void_p)), "set_params")
+
+    def train_step(self, x, target, lr: float, mask=None) -> float:
+        loss = C.c_float()
+        capi.check(self.L.wpf_net_train_step(self.h, _ptr(x), _ptr(target),
+                                             _ptr(mask) if mask is not None else None, lr,
+                                             C.byref(loss), None), "wpf_net_train_step")
+        return loss.value
+
+    def forward(self, x, out):
+        capi.check(self.L.wpf_net_forward(self.h, _ptr(x), _ptr(out), None), "wpf_net_forward")
+
+    def save(self, path: str, meta: dict | None = None):
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        np.savez_compressed(path, params=self.params(), meta=json.dumps(meta or {}))
+
+    @staticmethod
+    def load_params(path: str) -> np.ndarray:
+        with np.load(path) as z:
+            return z["params"]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wpf_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def attach(sim: Simulation, net: WarmStartNet | None):
+    """Use net (or none) as the learned start of sim's solves."""
+    capi.check(sim.L.wpf_set_warm_start_net(sim.h, net.h if net is not None else None),
+               "wpf_set_warm_start_net")
+
+
+def collect_pairs(sim: Simulation, steps: int, store: list, every: int = 1):
+    """Advance sim by `steps` steps, appending (input, target) device pairs for
+    the steps whose solve had two increments to extrapolate from."""
+    import torch
+    n = sim.params
+    nv = (n.nx // 2) * (n.ny // 2) * (n.nz // 2)
+    for s in range(steps):
+        take = (s % every == 0)
+        x = None
+        if take:
+            x = torch.empty(nv * 16, dtype=torch.int16, device="cuda")
+            rc = sim.L.wpf_ws_features(sim.h, sim.next_dtime(sim.itime + 1), _ptr(x))
+            if rc == capi.WPF_ERR_ARG:      # fewer than two increments yet
+                x = None
+            else:
+                capi.check(rc, "wpf_ws_features")
+        sim.step()
+        if x is not None:
+            t = torch.empty(nv, dtype=torch.float32, device="cuda")
+            capi.check(sim.L.wpf_ws_target(sim.h, _ptr(t)), "wpf_ws_target")
+            store.append((x, t))
+    return store
+
+
+def generate(runs: int, n: int, steps: int, spinup: int, seed0: int = 1000, every: int = 1,
+             log=print):
+    """Training pairs from `runs` seeded n^3 runs: log-K variance U(1, 3),
+    correlation length U(4, 16) cells; `spinup` steps are skipped first."""
+    rng = np.random.default_rng(seed0)
+    pairs = []
+    for r in range(runs):
+        lv, cl = float(rng.uniform(1.0, 3.0)), float(rng.uniform(4.0, 16.0))
+        case = make_case((n, n, n), log_var=lv, corr_len=cl, seed=seed0 + r)
+        with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                        rtol=1e-8, extrapolate=True) as sim:
+            for _ in range(spinup):
+                sim.step()
+            before = len(pairs)
+            collect_pairs(sim, steps, pairs, every)
+        log(f"run {r}: log-K var {lv:.2f} corr {cl:.1f}: {len(pairs) - before} pairs")
+    return pairs
+
+
+def train(net: WarmStartNet, pairs, epochs: int, lr: float, seed: int = 0, log=print):
+    rng = np.random.default_rng(seed)
+    hist = []
+    for ep in range(epochs):
+        order = rng.permutation(len(pairs))
+        tot = 0.0
+        for q in order:
+            x, t = pairs[q]
+            tot += net.train_step(x, t, lr)
+        hist.append(tot / max(len(pairs), 1))
+        log(f"epoch {ep}: mean loss {hist[-1]:.4e}")
+        lr *= 0.7
+    return hist
+
+
+def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int):
+    """Per-step stats of a run with the extrapolated start, with or without
+    the network: (relres0, inner iterations, warm_start code) per timed step."""
+    out = []
+    with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                    rtol=1e-8, extrapolate=True) as sim:
+        attach(sim, net)
+        for _ in range(spinup):
+            sim.step()
+        for _ in range(steps):
+            st = sim.step()
+            out.append((st.relres0, st.inner_iterations, st.warm_start))
+        attach(sim, None)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("--out", default=DEFAULT_WEIGHTS)
+    t.add_argument("--runs", type=int, default=20)
+    t.add_argument("--n", type=int, default=128)
+    t.add_argument("--steps", type=int, default=100)
+    t.add_argument("--spinup", type=int, default=10)
+    t.add_argument("--epochs", type=int, default=4)
+    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--eval-n", type=int, default=128)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    pairs = generate(a.runs, a.n, a.steps, a.spinup)
+    t1 = time.time()
+    net = WarmStartNet(a.n // 2, a.n // 2, a.n // 2, seed=a.seed)
+    hist = train(net, pairs, a.epochs, a.lr, a.seed)
+    t2 = time.time()
+    meta = {"runs": a.runs, "n": a.n, "steps": a.steps, "spinup": a.spinup, "epochs": a.epochs,
+            "lr": a.lr, "pairs": len(pairs), "loss": hist, "gen_s": t1 - t0, "train_s": t2 - t1}
+    net.save(a.out, meta)
+    print(json.dumps(meta))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,142 @@
+"""Long single-domain run through acid breakthrough, with its measurements.
+
+Breakthrough (no counterpart in the reference, whose showProgress computes
+the injected volume from the injection wells only, qinj = 0 under Dirichlet
+wells, wPFAW3D.f90:1784-1790): Q_in(t) = sum over the faces between ix = 1
+and 2 of u_x dx^2 (device reduction, wpf_diag.inlet_flux), PV_inj =
+integral of Q_in dt over the initial pore volume pv (:1695), and breakthrough
+is the first step at which a cell of the plane ix = nx - 1 has phase > 0
+(wpf_diag.phase_max_outlet).  Also reported: time-steps/s, Darcy-solve time
+and iterations, per-kernel-class device time and, for the HBM-bound stencil
+kernels, achieved GB/s from their algorithmic bytes; peak device memory.
+
+    python -m mizuho_edit_gb300.longrun --n 512 --steps 2000 --out run.json
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import statistics
+import time
+
+from . import capi
+from .cases import make_case
+from .sim import Simulation
+
+KC = ["permeability", "resid64", "coefficients", "smooth_l0", "mg_other", "apply", "pcg_vec",
+      "fused_update", "other", "bottom"]
+
+
+def run(n: int, steps: int, solver: str, extrapolate: bool, log_var: float, corr: float, seed: int,
+        stop_at_breakthrough: bool = False, timing: bool = True, learned_weights: str | None = None,
+        log=print):
+    import torch
+    case = make_case((n, n, n), log_var=log_var, corr_len=corr, seed=seed)
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    out = {"grid": [n, n, n], "solver": solver, "extrapolate": extrapolate, "log_var": log_var,
+           "corr_len": corr, "seed": seed}
+    net = None
+    with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver=solver, rtol=1e-8,
+                    extrapolate=extrapolate) as sim:
+        if learned_weights:
+            from . import learned
+            net = learned.WarmStartNet(n // 2, n // 2, n // 2)
+            net.set_params(learned.WarmStartNet.load_params(learned_weights))
+            learned.attach(sim, net)
+        L = sim.L
+        if timing:
+            capi.check(L.wpf_set_kernel_timing(sim.h, (1 << len(KC)) - 1), "timing")
+        d0 = sim.diagnostics()
+        pv = d0["pv"]
+        vin, q_prev = 0.0, d0["inlet_flux"]
+        bt = None
+        its, solve_ms, relres0, ws = [], [], [], []
+        min_free = free0
+        t0 = time.perf_counter()
+        for s in range(steps):
+            st = sim.step()
+            its.append(st.inner_iterations)
+            solve_ms.append(st.solve_ms)
+            relres0.append(st.relres0)
+            ws.append(st.warm_start)
+            d = sim.diagnostics()
+            q = d["inlet_flux"]
+            vin += 0.5 * (q + q_prev) * st.dtime          # trapezoid in time
+            q_prev = q
+            if bt is None and d["phase_max_outlet"] > 0.0:
+                bt = {"step": s + 1, "time": sim.time, "pv_injected": vin / pv}
+                log(f"breakthrough at step {s + 1}: PV_inj {vin / pv:.5f}")
+                if stop_at_breakthrough:
+                    break
+            if (s + 1) % 200 == 0:
+                free, _ = torch.cuda.mem_get_info()
+                min_free = min(min_free, free)
+                log(f"step {s + 1}: t {sim.time:.4g} PV_inj {vin / pv:.4f} its {st.inner_iterations} "
+                    f"relres0 {st.relres0:.2e}")
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        free, _ = torch.cuda.mem_get_info()
+        min_free = min(min_free, free)
+        nb = C.c_int64()
+        L.wpf_device_bytes(sim.h, C.byref(nb))
+        kms = (C.c_double * len(KC))()
+        kcnt = (C.c_int64 * len(KC))()
+        L.wpf_kernel_times(sim.h, kms, kcnt, len(KC))
+        done = len(its)
+        cells = n ** 3
+        out.update({
+            "steps": done, "time": sim.time, "wall_s": wall,
+            "time_steps_per_s_incl_diagnostics": done / wall,
+            "darcy_solve_ms_mean": statistics.mean(solve_ms),
+            "pcg_iterations_mean": statistics.mean(its),
+            "relres0_mean": statistics.mean(relres0),
+            "warm_start_codes": {str(c): ws.count(c) for c in sorted(set(ws))},
+            "breakthrough": bt, "pv": pv, "pv_injected_end": vin / pv,
+            "device_bytes_library": nb.value,
+            "peak_device_bytes_used": int(free0 - min_free) + (total - free0),
+            "hbm_total_bytes": total,
+        })
+        if timing:
+            ms = {KC[c]: float(kms[c]) for c in range(len(KC))}
+            out["kernel_class_ms_per_step"] = {k: v / done for k, v in ms.items()}
+            # algorithmic bytes per cell of the HBM-bound stencil kernels (FP32 solver)
+            cnt = int(kcnt[3])
+            if ms["smooth_l0"] > 0 and cnt:
+                cyc = cnt // 4
+                b = (cyc * 24.0 + (cnt - cyc) * 28.0 + cyc * 0.5) * cells
+                out["smooth_l0_gbs"] = b / (ms["smooth_l0"] / 1e3) / 1e9
+            if ms["apply"] > 0:
+                out["apply_gbs"] = int(kcnt[5]) * 32.0 * cells / (ms["apply"] / 1e3) / 1e9
+        if net is not None:
+            from . import learned
+            learned.attach(sim, None)
+            net.close()
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-extrapolate", action="store_true")
+    ap.add_argument("--log-var", type=float, default=2.5)
+    ap.add_argument("--corr", type=float, default=16.0)
+    ap.add_argument("--seed", type=int, default=512)
+    ap.add_argument("--stop-at-breakthrough", action="store_true")
+    ap.add_argument("--learned", default=None, help="weights of the learned start (npz)")
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    res = run(a.n, a.steps, a.solver, not a.no_extrapolate, a.log_var, a.corr, a.seed,
+              a.stop_at_breakthrough, learned_weights=a.learned)
+    s = json.dumps(res)
+    print(s)
+    if a.out:
+        with open(a.out, "w") as fh:
+            fh.write(s + "\n")
+
+
+if __name__ == "__main__":
+    main()

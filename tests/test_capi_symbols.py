@@ -1,5 +1,5 @@
 """The C-ABI library builds for sm_103a here (nvcc cross-compiles), loads, and
-exports every entry point include/wpf.h declares.  No compute calls: there is
+exports every entry point include/*.h declares.  No compute calls: there is
 no GPU in this container, so only the failure path of wpf_create is called."""
 import ctypes as C
 import os
@@ -11,9 +11,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    txt = open(os.path.join(ROOT, "include", "wpf.h")).read()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(wpf_[a-z0-9_]+)\s*\(", txt)))
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            txt = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+            names |= set(re.findall(r"\b(wpf_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
 
 
 def test_header_declares_the_reference_routines():

@@ -1,0 +1,73 @@
+"""The learned warm start inside the solve: data generation from the simulator,
+training on the GPU, and what the trained network gains over the
+extrapolated start without it -- with every solve still finishing at the same
+FP64 residual tolerance and the same answer."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _mods():
+    from mizuho_edit_gb300 import learned
+    from mizuho_edit_gb300.cases import make_case
+    from mizuho_edit_gb300.sim import Simulation
+    return learned, make_case, Simulation
+
+
+def test_net_start_same_solution():
+    """An attached (untrained) network changes only the start: 12 steps agree
+    with the run without it to the solver tolerance, every solve converges."""
+    learned, make_case, Simulation = _mods()
+    case = make_case((32, 32, 32), log_var=2.0, corr_len=5.0, seed=31)
+    out = {}
+    for use in (False, True):
+        net = learned.WarmStartNet(16, 16, 16, seed=3) if use else None
+        with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
+                        rtol=1e-8, extrapolate=True) as sim:
+            learned.attach(sim, net)
+            st = [sim.step() for _ in range(12)]
+            learned.attach(sim, None)
+            assert all(s.converged and s.relres <= 1e-8 for s in st)
+            out[use] = (st, sim.download("pressure", "phase", "concent"))
+        if net is not None:
+            codes = [s.warm_start for s in st]
+            # no history on the first solve; later: the net's start (2), the
+            # extrapolation's (1) or, in the start-up transient, p itself (-1)
+            assert codes[0] == 0 and set(codes[3:]) <= {-1, 1, 2}
+            net.close()
+    for k in ("pressure", "phase", "concent"):
+        assert rel_l2(out[True][1][k], out[False][1][k]) < 1e-6, k
+
+
+def test_trained_net_gains_over_extrapolation():
+    """Train on pairs the simulator generates (6 seeded 128^3 runs), then on
+    an unseen seed: the network predicts the extrapolation's error (held-out
+    loss well below that of predicting zero, which is the start without it),
+    and its start leaves a residual no larger than the extrapolation's."""
+    import torch
+    learned, make_case, Simulation = _mods()
+    pairs = learned.generate(6, 128, 40, 10, seed0=500, log=lambda *a: None)
+    held = learned.generate(1, 128, 12, 30, seed0=900, log=lambda *a: None)
+    assert len(pairs) >= 200 and len(held) >= 10
+    net = learned.WarmStartNet(64, 64, 64, seed=1)
+    hist = learned.train(net, pairs, 4, 2e-3, log=lambda *a: None)
+    assert hist[-1] < hist[0]
+    out = torch.empty(64 ** 3, dtype=torch.float32, device="cuda")
+    zero, err = [], []
+    for x, t in held:
+        net.forward(x, out)
+        err.append(float(((out - t).double() ** 2).mean()))
+        zero.append(float((t.double() ** 2).mean()))
+    assert np.mean(err) < 0.5 * np.mean(zero)
+    case = make_case((128, 128, 128), log_var=2.0, corr_len=8.0, seed=901)
+    base = learned.evaluate(case, None, 10, 30)
+    with_net = learned.evaluate(case, net, 10, 30)
+    r_base = np.mean([s[0] for s in base])
+    r_net = np.mean([s[0] for s in with_net])
+    assert all(s[2] in (-1, 1, 2) for s in with_net)
+    assert sum(s[2] == 2 for s in with_net) >= 5
+    assert r_net <= r_base * (1 + 1e-3)
+    net.close()
