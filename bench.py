@@ -148,6 +148,19 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def sweep_traffic_per_cell():
+    """DRAM bytes per cell per launch of the finest-level sweep, averaged over
+    a cycle, as measured by ncu (profiles/k_sweep_async_224.md)."""
+    try:
+        with open(os.path.join(HERE, "profiles", "k_sweep_async_224.md")) as fh:
+            for line in fh:
+                if line.startswith("traffic_bytes_per_cell_avg"):
+                    return float(line.split("=")[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def make_workload(args, rank):
     from mizuho_edit_gb300.cases import make_case
     n = args.n
@@ -272,9 +285,14 @@ def run_ours(args):
         kname, per_cell = "k_rbgs<float> (finest level)", 20
     peak, peak_kind = measured_peaks()
     achieved = smooth_bytes / (smooth_ms / 1000.0) / 1e9 if smooth_ms > 0 else None
+    traffic = None   # DRAM bytes per launch, from the ncu capture summarised in profiles/
+    if ncell >= (1 << 23):
+        tpc = sweep_traffic_per_cell()
+        traffic = tpc * ncell if tpc else None
     roof = {"kernel": kname, "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "traffic_source": "profiles/k_sweep_async_224.md (ncu, 224^3, scaled by cells)",
             "peak_source": peak_kind, "bytes_per_cell_per_launch": per_cell,
             "launches": cnt, "avg_launch_us": smooth_ms * 1000.0 / max(cnt, 1)}
 

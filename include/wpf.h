@@ -238,6 +238,18 @@ int wpf_host_free(void* ptr);
 int wpf_snapshot(wpf_handle* h, float* out);
 int wpf_snapshot_wait(wpf_handle* h);
 
+/* Ensemble of independent domains (no counterpart in the reference, which
+ * runs one domain): nsteps wpf_step calls on each of the n members (steps
+ * itime0 .. itime0+nsteps-1), dtime[m] in/out per member as for wpf_step,
+ * stats[m] (may be NULL) the last step's.  A pool of nthreads host threads
+ * owns the members round-robin; each member runs on its own stream, so the
+ * kernels of some members fill the GPU while others wait on a read-back.
+ * status[m] (may be NULL) gets each member's status; a member that failed
+ * stops.  Returns WPF_OK, or the first failure other than
+ * WPF_ERR_NOT_CONVERGED, else that.                                         */
+int wpf_ensemble_run(wpf_handle** members, int32_t n, int32_t itime0, int32_t nsteps, int32_t nthreads,
+                     double* dtime, wpf_step_stats* stats, int32_t* status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,8 @@ LIB_NAME = "libwpf_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["wpf_capi.cu", "wpf_physics.cu", "wpf_solver.cu", "wpf_noalloc.cu", "wpf_net.cu"]
+SOURCES = ["wpf_capi.cu", "wpf_physics.cu", "wpf_solver.cu", "wpf_noalloc.cu", "wpf_net.cu",
+           "wpf_ensemble.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

@@ -113,6 +113,8 @@ SIGNATURES = {
     "wpf_host_free": (C.c_int, [C.c_void_p]),
     "wpf_snapshot": (C.c_int, [H, C.c_void_p]),
     "wpf_snapshot_wait": (C.c_int, [H]),
+    "wpf_ensemble_run": (C.c_int, [C.POINTER(H), C.c_int32, C.c_int32, C.c_int32, C.c_int32, DP,
+                                   C.POINTER(StepStats), C.POINTER(C.c_int32)]),
     # include/wpf_net.h: the learned warm start
     "wpf_net_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "wpf_net_destroy": (C.c_int, [C.c_void_p]),
