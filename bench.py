@@ -62,6 +62,8 @@ def parse():
                     help="launch the preconditioner cycle kernel by kernel")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 MG-PCG comparison run")
+    ap.add_argument("--no-tma", action="store_true",
+                    help="stage the finest-level sweep with cp.async instead of bulk-tensor copies")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the run with the learned correction of the start")
     ap.add_argument("--spinup", type=int, default=40,
@@ -79,7 +81,7 @@ def solver_kwargs(args, solver=None):
     plain = solver == "fp64"
     return dict(solver=solver or args.solver, rtol=args.rtol, w_from_level=args.w_from,
                 smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min,
-                graphs=not args.no_graphs,
+                graphs=not args.no_graphs, tma=not args.no_tma,
                 extrapolate=(not plain) and args.warm_start == "extrap")
 
 

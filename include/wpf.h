@@ -98,6 +98,9 @@ typedef struct wpf_solver_opts {
  * The increment history survives wpf_upload and is cleared by wpf_set_wells
  * and wpf_set_solver.  No counterpart in the reference.                    */
 #define WPF_SOLVER_EXTRAPOLATE 2
+/* WPF_SOLVER_NO_TMA: stage the finest-level sweep with per-thread cp.async
+ * copies instead of bulk-tensor (TMA) copies (same arithmetic, same results). */
+#define WPF_SOLVER_NO_TMA 4
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

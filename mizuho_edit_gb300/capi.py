@@ -26,6 +26,7 @@ SOLVER_FP64 = 0
 SOLVER_MIXED = 1
 SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bits
 SOLVER_EXTRAPOLATE = 2
+SOLVER_NO_TMA = 4
 
 
 class WpfError(RuntimeError):

@@ -10,6 +10,7 @@
 // of an FP64 field.  The padding columns are allocated but never read.
 #pragma once
 
+#include <cuda.h>   // CUtensorMap
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -64,6 +65,7 @@ enum Slot {
     S_WSD2,             // sum of the squared change of the increment (its output scale)
     S_DPH2,             // sum of the squared phase change of the last step (its scale)
     S_KLOG0, S_KLOG1,   // sum of log K_rock and of its square (input normalisation)
+    S_KERR,             // set (int) by a kernel whose bounded wait ran out
     S_COUNT = 32
 };
 
@@ -88,10 +90,19 @@ struct Level {
 
 constexpr int MAX_LEVELS = 16;
 
+// Bulk-tensor maps of one level for the TMA-staged sweep kernel: the x input
+// and the five operator arrays (cx, cy, cz, 1/diag, b).
+struct SweepMaps {
+    CUtensorMap x, cx, cy, cz, id, b;
+};
+
 template <typename R>
 struct Hierarchy {
     int nlev = 0;
     Level<R> lv[MAX_LEVELS];
+    // per level: maps with the x input in xs ([0]) or in x ([1]); tm_ok when encoded
+    SweepMaps tm[MAX_LEVELS][2];
+    bool tm_ok[MAX_LEVELS] = {};
     // PCG vectors on the fine grid (level 0 aliases: lv[0].b = r, lv[0].x = z);
     // p is double buffered (p, p2) because the operator kernel forms the new
     // search direction of a cell's neighbours on the fly from z and the old p.

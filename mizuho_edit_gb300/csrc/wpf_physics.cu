@@ -46,6 +46,29 @@ __device__ __forceinline__ bool phase_uniform(const double* __restrict__ ph, lon
            bits(ph[n - 1 + sz]) == b0 && bits(ph[n + 1 - sz]) == b0 && bits(ph[n - 1 - sz]) == b0;
 }
 
+// The same two tests with every load issued before any comparison (no
+// short circuit), so a thread keeps its 26 loads in flight together: the
+// classification kernel touches every cell and is bound by memory latency.
+__device__ __forceinline__ bool phase_uniform_eager(const double* __restrict__ ph, long long n,
+                                                    long long sy, long long sz) {
+    const long long o[18] = {1, -1, sy, -sy, sz, -sz, 1 + sy, 1 - sy, -1 + sy, -1 - sy, sy + sz, -sy + sz,
+                             sy - sz, -sy - sz, 1 + sz, -1 + sz, 1 - sz, -1 - sz};
+    long long v[18];
+    const long long b0 = bits(ph[n]);
+#pragma unroll
+    for (int q = 0; q < 18; ++q) v[q] = bits(ph[n + o[q]]);
+    long long diff = 0;
+#pragma unroll
+    for (int q = 0; q < 18; ++q) diff |= v[q] ^ b0;
+    return diff == 0 && (b0 & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool concent_zero_eager(const double* __restrict__ C, long long n, long long sy,
+                                                   long long sz) {
+    const long long a = bits(C[n]) | bits(C[n + 1]) | bits(C[n - 1]) | bits(C[n + sy]) | bits(C[n - sy]) |
+                        bits(C[n + sz]) | bits(C[n - sz]);
+    return (a << 1) == 0;
+}
+
 // Face velocities around a cell: u_{x+}, u_{x-}, u_{y+}, u_{y-}, u_{z+}, u_{z-}.
 struct FaceVel {
     double xp, xm, yp, ym, zp, zm;
@@ -402,8 +425,9 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const bool well = (fl[n] & F_WELL) != 0;
-        const bool uni = phase_uniform(ph, n, sy, sz);
-        const bool copy = uni && (well || concent_zero(cc, n, sy, sz));
+        const bool uni = phase_uniform_eager(ph, n, sy, sz);
+        const bool cz0 = concent_zero_eager(cc, n, sy, sz);
+        const bool copy = uni && (well || cz0);
         if (copy) {
             const double a = ph[n], c = cc[n];
             ph_out[n] = a;

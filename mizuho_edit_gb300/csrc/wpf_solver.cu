@@ -37,7 +37,9 @@
 // reads x from one buffer and writes the other, so no block can see another
 // block's new values.  Mid-size levels use in-place two-kernel half-sweeps and
 // the levels of at most 4096 cells run their whole sub-cycle in one block.
+#include <cuda.h>   // CUtensorMap (the encoder is fetched at run time)
 #include <math.h>
+#include <stddef.h>
 #include <stdio.h>
 
 #include "wpf_internal.cuh"
@@ -328,16 +330,69 @@ constexpr int NSLOT = 7;
 constexpr int R1X = SX + 2, R1Y = SY + 2;   // first-colour region: tile + 1-cell ring
 constexpr int WX = SX + 8;                  // staged row: i in [i0-4, i0+SX+3], 16-byte aligned
 
+// Each array starts on a 128-byte boundary: the bulk-tensor copies write
+// whole boxes there.
 template <typename R>
-struct SweepSlot {
-    R x[FY][WX];             // rows j in [j0-2, j0+SY+1]
-    R cx[R1Y][WX];           // rows j in [j0-1, j0+SY]
-    R cy[R1Y + 1][WX];       // rows j in [j0-2, j0+SY]
-    R cz[R1Y][WX];
-    R id[R1Y][WX];
-    R b[R1Y][WX];
+struct alignas(128) SweepSlot {
+    alignas(128) R x[FY][WX];         // rows j in [j0-2, j0+SY+1]
+    alignas(128) R cx[R1Y][WX];       // rows j in [j0-1, j0+SY]
+    alignas(128) R cy[R1Y + 1][WX];   // rows j in [j0-2, j0+SY]
+    alignas(128) R cz[R1Y][WX];
+    alignas(128) R id[R1Y][WX];
+    alignas(128) R b[R1Y][WX];
 };
 constexpr int SLOT_ROWS = FY + R1Y + (R1Y + 1) + 3 * R1Y;   // 63 staged rows per plane
+
+// element offset in a slot of staged row `row` (rows numbered x, cx, cy, cz, id, b)
+template <typename R>
+__device__ __forceinline__ int slot_row_offset(int row) {
+    typedef SweepSlot<R> S;
+    if (row < FY) return (int)(offsetof(S, x) / sizeof(R)) + row * WX;
+    row -= FY;
+    if (row < R1Y) return (int)(offsetof(S, cx) / sizeof(R)) + row * WX;
+    row -= R1Y;
+    if (row < R1Y + 1) return (int)(offsetof(S, cy) / sizeof(R)) + row * WX;
+    row -= R1Y + 1;
+    if (row < R1Y) return (int)(offsetof(S, cz) / sizeof(R)) + row * WX;
+    row -= R1Y;
+    if (row < R1Y) return (int)(offsetof(S, id) / sizeof(R)) + row * WX;
+    return (int)(offsetof(S, b) / sizeof(R)) + (row - R1Y) * WX;
+}
+
+// SweepMaps (wpf_internal.cuh): the x input (12-row boxes), cx / cz / 1/diag /
+// b (10-row boxes) and cy (11-row boxes), each box WX elements wide; 3-D
+// tensors (P, ny+2, nz+2) over the pitched arrays.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(map), "r"(x), "r"(y), "r"(z),
+        "r"((unsigned)__cvta_generic_to_shared(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    for (int it = 0; it < (1 << 20); ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool ok) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -352,9 +407,12 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // x += x_{l+1}(parent) fused into the staged x.  dot != null: accumulate b.xout.
 // Every staged row is a 16-byte aligned window of WX elements starting at
 // i = i0 - 4 (XOFF and the pitches make at(i0-4, j, k) a multiple of 4
-// elements); each thread owns fixed 16-byte chunks of the slot, so its copy
-// addresses are precomputed once and advanced by one plane stride per plane.
-template <typename R, bool ZERO>
+// elements).  TMA: one thread stages a plane with five or six bulk-tensor
+// copies that complete on the slot's mbarrier (zero fill outside the halo
+// box); otherwise each thread owns fixed 16-byte chunks of the slot and
+// copies them with cp.async, its addresses precomputed once and advanced by
+// one plane stride per plane.
+template <typename R, bool ZERO, bool TMA>
 __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __restrict__ cx,
                                                          const R* __restrict__ cy,
                                                          const R* __restrict__ cz,
@@ -363,9 +421,26 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
                                                          const R* __restrict__ xin,
                                                          R* __restrict__ xout, int c0,
                                                          const R* __restrict__ xc, Grid gc,
-                                                         double* dot) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SweepSlot<R>* slots = reinterpret_cast<SweepSlot<R>*>(smem_raw);
+                                                         double* dot,
+                                                         const __grid_constant__ SweepMaps maps,
+                                                         int* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t mbar[NSLOT];
+    // slots on a 128-byte boundary whatever the dynamic window's base (the
+    // allocation carries 128 spare bytes)
+    const unsigned mis = (unsigned)__cvta_generic_to_shared(smem_raw) & 127u;
+    SweepSlot<R>* slots = reinterpret_cast<SweepSlot<R>*>(smem_raw + (mis ? 128u - mis : 0u));
+    if (TMA) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            for (int q = 0; q < NSLOT; ++q)
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                                 (unsigned)__cvta_generic_to_shared(&mbar[q]))
+                             : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
+    bool wait_ok = true;
     constexpr int NT = SX * SY;
     constexpr int EPC = 16 / sizeof(R);               // elements per 16-byte chunk
     constexpr int CPR = WX / EPC;                     // chunks per staged row
@@ -412,24 +487,46 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         ci[s] = e0;
         cx_ok[s] = j >= 0 && j <= g.ny + 1 && e0 <= g.nx + 1;
         coff[s] = XOFF + (long long)j * g.P + e0;
-        csm[s] = srow * WX + ch * EPC;
+        csm[s] = slot_row_offset<R>(srow) + ch * EPC;
     }
-    auto slot_base = [&](int k) -> R* {
-        return reinterpret_cast<R*>(&slots[(k + 2 * NSLOT) % NSLOT]);
-    };
-    auto slot = [&](int k) -> SweepSlot<R>& { return slots[(k + 2 * NSLOT) % NSLOT]; };
+    auto slot_index = [&](int k) { return (k + 2 * NSLOT) % NSLOT; };
+    auto slot_base = [&](int k) -> R* { return reinterpret_cast<R*>(&slots[slot_index(k)]); };
+    auto slot = [&](int k) -> SweepSlot<R>& { return slots[slot_index(k)]; };
     auto issue = [&](int k) {
         R* base = slot_base(k);
+        if (TMA) {
+            // the zero-guess sweep stages no x: its rows are zeroed here
+            if (ZERO) {
+#pragma unroll
+                for (int s = 0; s < MAXC; ++s)
+                    if (cis_x[s]) {
+#pragma unroll
+                        for (int e = 0; e < EPC; ++e) base[csm[s] + e] = 0;
+                    }
+            }
+            if (tid == 0) {
+                SweepSlot<R>& S = slots[slot_index(k)];
+                uint64_t* bar = &mbar[slot_index(k)];
+                constexpr unsigned rowb = WX * sizeof(R);
+                mbar_expect(bar, rowb * (ZERO ? (SLOT_ROWS - FY) : SLOT_ROWS));
+                const int x0 = XOFF + i0 - 4;
+                if (!ZERO) tma_load_3d(&S.x[0][0], &maps.x, x0, j0 - 2, k, bar);
+                tma_load_3d(&S.cx[0][0], &maps.cx, x0, j0 - 1, k, bar);
+                tma_load_3d(&S.cy[0][0], &maps.cy, x0, j0 - 2, k, bar);
+                tma_load_3d(&S.cz[0][0], &maps.cz, x0, j0 - 1, k, bar);
+                tma_load_3d(&S.id[0][0], &maps.id, x0, j0 - 1, k, bar);
+                tma_load_3d(&S.b[0][0], &maps.b, x0, j0 - 1, k, bar);
+            }
+            return;
+        }
         const bool kok = k >= 0 && k <= g.nz + 1;
 #pragma unroll
         for (int s = 0; s < MAXC; ++s) {
             if (!csrc[s] && !(ZERO && cis_x[s])) continue;
             if (ZERO && cis_x[s]) {
-                if (cj[s] >= 0 || true) {
-                    R* d = base + csm[s];
+                R* d = base + csm[s];
 #pragma unroll
-                    for (int e = 0; e < EPC; ++e) d[e] = 0;
-                }
+                for (int e = 0; e < EPC; ++e) d[e] = 0;
                 continue;
             }
             const bool ok = kok && cx_ok[s];
@@ -437,6 +534,12 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             cp_async16(base + csm[s], src, ok);
         }
         cp_async_commit();
+    };
+    // plane k staged (TMA: the fill number of its slot gives the phase parity);
+    // after one wait has run out the block stops waiting and reports it
+    auto landed = [&](int k) {
+        if (!wait_ok) return;
+        if (!mbar_wait_bounded(&mbar[slot_index(k)], (unsigned)(((k - (k0 - 2)) / NSLOT) & 1))) wait_ok = false;
     };
     // after plane k has landed: add the coarse correction to this thread's x chunks
     auto correct = [&](int k) {
@@ -503,15 +606,21 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     };
 
     for (int k = k0 - 2; k <= k0 + 3; ++k) issue(k);
-    cp_async_wait<2>();                       // planes k0-2 .. k0+1 landed
+    if (TMA) {
+        for (int k = k0 - 2; k <= k0 + 1; ++k) landed(k);
+    } else {
+        cp_async_wait<2>();                   // planes k0-2 .. k0+1 landed
+    }
     for (int k = k0 - 2; k <= k0 + 1; ++k) correct(k);
     __syncthreads();
     first_colour(k0 - 1);
     __syncthreads();
     first_colour(k0);
     for (int k = k0; k <= k1; ++k) {
+        if (TMA) fence_proxy_async();         // this thread's generic accesses before the next copies
         issue(k + 4);                         // the slot of plane k-3, idle since k-2
-        cp_async_wait<2>();                   // plane k+2 landed
+        if (TMA) landed(k + 2);
+        else cp_async_wait<2>();              // plane k+2 landed
         correct(k + 2);
         __syncthreads();
         if (k > k0) write_out(k - 1);
@@ -521,12 +630,18 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     }
     __syncthreads();
     write_out(k1);
-    cp_async_wait<0>();
+    if (TMA) {   // the copies still in flight land before the block exits
+        landed(k1 + 3);
+        landed(k1 + 4);
+        if (!wait_ok && err) atomicExch(err, 1);
+    } else {
+        cp_async_wait<0>();
+    }
     if (dot) block_add(dacc, dot);
 }
 
 template <typename R>
-constexpr size_t sweep_smem() { return sizeof(SweepSlot<R>) * NSLOT; }
+constexpr size_t sweep_smem() { return sizeof(SweepSlot<R>) * NSLOT + 128; }
 
 // One colour of red-black Gauss-Seidel in place (mid-size levels).  Thread
 // (t,j,k) handles the cell of colour `color` at i = 1 + 2t + ((color+1+j+k) & 1).
@@ -943,6 +1058,86 @@ constexpr long long BIG_CELLS = 1LL << 23;   // default: levels swept by the pip
 // pre-sweep writes xs, the last post-sweep writes x); mid levels sweep x in
 // place; the levels from the first one with at most bottom_cells<R>() cells
 // run in one k_bottom block.
+// ---- bulk-tensor maps of the sweep -------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// 3-D map (x over the whole pitched row, y = j in 0..ny+1, z = k in 0..nz+1)
+// with boxes of WX x rows x 1 elements; outside the tensor the copy fills zeros.
+template <typename R>
+static bool encode_map(CUtensorMap* m, const R* base, const Grid& g, int rows) {
+    const EncodeTiledFn f = tensor_map_encoder();
+    if (!f || !base) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.P, (cuuint64_t)(g.ny + 2), (cuuint64_t)(g.nz + 2)};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.P * sizeof(R), (cuuint64_t)g.S * sizeof(R)};
+    const cuuint32_t box[3] = {(cuuint32_t)WX, (cuuint32_t)rows, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return f(m, sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+             (void*)base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <typename R>
+static bool ensure_maps(Hierarchy<R>& H, int l) {
+    if (H.tm_ok[l]) return true;
+    const Level<R>& L = H.lv[l];
+    bool ok = true;
+    for (int v = 0; v < 2; ++v) {
+        SweepMaps& m = H.tm[l][v];
+        ok = ok && encode_map(&m.x, v ? L.x : L.xs, L.g, FY) && encode_map(&m.cx, L.cx, L.g, R1Y) &&
+             encode_map(&m.cy, L.cy, L.g, R1Y + 1) && encode_map(&m.cz, L.cz, L.g, R1Y) &&
+             encode_map(&m.id, L.idiag, L.g, R1Y) && encode_map(&m.b, L.b, L.g, R1Y);
+    }
+    H.tm_ok[l] = ok;
+    return ok;
+}
+
+// One sweep of level l from `in` to `out` (the TMA-staged kernel unless the
+// maps are unavailable or the caller asked for the cp.async one).
+template <typename R>
+static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool zero, const R* in, R* out,
+                         int c0, const R* xc, const Grid& gc, double* dot) {
+    Level<R>& L = H.lv[l];
+    const Grid& g = L.g;
+    cudaStream_t s = h->stream;
+    const dim3 sb(SX, SY);
+    const bool tma = !(h->opts.flags & WPF_SOLVER_NO_TMA) && ensure_maps(H, l);
+    const SweepMaps& m = H.tm[l][in == L.x ? 1 : 0];
+    int* err = reinterpret_cast<int*>(h->dsc + S_KERR);
+    const size_t sm = sweep_smem<R>();
+    if (tma && zero)
+        WPF_LAUNCH(h, cls, k_sweep_async<R, true, true><<<sweep_grid(g), sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+    else if (tma)
+        WPF_LAUNCH(h, cls, k_sweep_async<R, false, true><<<sweep_grid(g), sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+    else if (zero)
+        WPF_LAUNCH(h, cls, k_sweep_async<R, true, false><<<sweep_grid(g), sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+    else
+        WPF_LAUNCH(h, cls, k_sweep_async<R, false, false><<<sweep_grid(g), sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+}
+
 template <typename R>
 static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, long long big,
                         int wfrom, double* rz, bool& need_dot) {
@@ -982,12 +1177,7 @@ static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, l
         for (int it = 0; it < nu; ++it) {
             const R* in = buf[(it + 1) & 1];
             R* out = buf[it & 1];
-            if (it == 0)
-                WPF_LAUNCH(h, cls, k_sweep_async<R, true><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
-            else
-                WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                    g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 0, nullptr, g, nullptr));
+            launch_sweep(h, H, l, cls, it == 0, in, out, 0, (const R*)nullptr, g, nullptr);
         }
         const R* pre_end = buf[(nu - 1) & 1];
         WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
@@ -999,9 +1189,8 @@ static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, l
             R* out = buf[w & 1];
             const bool last0 = (l == 0 && it == nu - 1 && rz);
             if (last0) need_dot = false;
-            WPF_LAUNCH(h, cls, k_sweep_async<R, false><<<sweep_grid(g), sb, sweep_smem<R>(), s>>>(
-                g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, 1, it == 0 ? C.x : nullptr, C.g,
-                last0 ? rz : nullptr));
+            launch_sweep(h, H, l, cls, false, in, out, 1, it == 0 ? (const R*)C.x : nullptr, C.g,
+                         last0 ? rz : nullptr);
         }
         return;
     }
@@ -1171,9 +1360,13 @@ template <typename R>
 static int set_sweep_smem() {
     WPF_CUDA(cudaFuncSetAttribute(k_bottom<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)BOTTOM_SMEM_MAX));
-    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sweep_smem<R>()));
-    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sweep_smem<R>()));
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sweep_smem<R>()));
+    WPF_CUDA(cudaFuncSetAttribute(k_sweep_async<R, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sweep_smem<R>()));
     return WPF_OK;
 }
@@ -1400,8 +1593,18 @@ int solve_pressure(wpf_handle* h, wpf_step_stats* st) {
     else rc = solve_impl(h, h->h64, st);
     int rc2 = phys_halo(h, h->pressure);   // updateHalo(pressure), :1050
     WPF_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    // a sweep whose bounded staging wait ran out left its flag
+    WPF_CUDA(cudaMemcpyAsync(h->hsc + S_KERR, h->dsc + S_KERR, sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    WPF_CUDA(cudaEventSynchronize(h->ev[1]));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    int kerr = 0;
+    memcpy(&kerr, h->hsc + S_KERR, sizeof(int));
+    if (kerr) {
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KERR, 0, sizeof(double), h->stream));
+        rc = WPF_ERR_TIMEOUT;
+    }
     if (st) {
-        WPF_CUDA(cudaEventSynchronize(h->ev[1]));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
         st->solve_ms = ms;

@@ -255,6 +255,30 @@ def test_pipelined_sweep_matches_half_sweeps(oracle_mod):
     assert rel_l2(out["pipelined"][1], out["half"][1]) < 1e-9
 
 
+@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+def test_tma_staged_sweep_matches_cp_async(oracle_mod, solver):
+    """The pipelined sweep staged by bulk-tensor (TMA) copies does the same
+    arithmetic as the cp.async-staged one: same iterations, same pressure up
+    to the order of the block-sum atomics.  Threshold 1 forces the pipelined
+    kernel on every level above the single-block bottom (128x96x64 down to
+    32x24x16), so ragged tiles in y and z and both zero-guess and prolonging
+    sweeps are covered."""
+    _, Simulation = _sim_mod()
+    case = _case((128, 96, 64), seed=27, log_var=2.0, corr_len=6.0)
+    p = case.params
+    out = {}
+    for tma in (True, False):
+        with Simulation(p, case.permeab_rock, case.phase, case.concent, solver=solver,
+                        rtol=1e-10, sweep_min_cells=1, tma=tma) as sim:
+            st = [sim.step() for _ in range(3)]
+            assert all(s.converged for s in st)
+            out[tma] = ([s.inner_iterations for s in st], sim.download("pressure"),
+                        sim.download("phase"))
+    assert all(abs(a - b) <= 1 for a, b in zip(out[True][0], out[False][0]))
+    assert rel_l2(out[True][1], out[False][1]) < 1e-9
+    assert rel_l2(out[True][2], out[False][2]) < 1e-9
+
+
 def test_extrapolated_start_same_solution_fewer_iterations(oracle_mod):
     """The time-extrapolated start changes only where each solve begins: over
     30 steps the fields agree with the run from the previous pressure to the
