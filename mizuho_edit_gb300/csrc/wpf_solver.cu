@@ -260,12 +260,15 @@ __global__ void __launch_bounds__(RB) k_l0_coeffs(Grid g, const double* __restri
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const bool live = !(fl[n] & F_DIR);
-        const double tx = Tx[n], ty = Ty[n], tz = Tz[n];
-        const double d = tx + Tx[n - 1] + ty + Ty[n - sy] + tz + Tz[n - sz];
-        cx[n] = (R)((live && !(fl[n + 1] & F_DIR)) ? tx : 0.0);
-        cy[n] = (R)((live && !(fl[n + sy] & F_DIR)) ? ty : 0.0);
-        cz[n] = (R)((live && !(fl[n + sz] & F_DIR)) ? tz : 0.0);
-        const R dr = (R)(live ? d : 0.0);
+        // each face converted once; the diagonal sums the six faces in R: FP64
+        // issue is scarce, and the FP32 operator only needs FP32 accuracy (the
+        // outer residual is FP64)
+        const R tx = (R)Tx[n], ty = (R)Ty[n], tz = (R)Tz[n];
+        cx[n] = (live && !(fl[n + 1] & F_DIR)) ? tx : (R)0;
+        cy[n] = (live && !(fl[n + sy] & F_DIR)) ? ty : (R)0;
+        cz[n] = (live && !(fl[n + sz] & F_DIR)) ? tz : (R)0;
+        const R d = tx + (R)Tx[n - 1] + ty + (R)Ty[n - sy] + tz + (R)Tz[n - sz];
+        const R dr = live ? d : (R)0;
         diag[n] = dr;
         idiag[n] = (live && dr > (R)0) ? (R)1 / dr : (R)0;
     }
@@ -569,39 +572,46 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
                  S.cz[c][w] * Sp.x[c + 1][w] + Sm.cz[c][w] * Sm.x[c + 1][w];
         return S.id[c][w] * s;
     };
-    // First colour of plane k on the tile + ring: thread t < 17*R1Y takes the
+    // Per-thread constants of the three compute phases (the colour of a cell
+    // flips with the plane parity only).
+    // First colour of a plane on the tile + ring: thread t < 17*R1Y takes the
     // m-th cell of that colour in R1 row c (every other cell of the row).
-    auto first_colour = [&](int k) {
-        constexpr int PER_ROW = R1X / 2;
-        if (k < 1 || k > g.nz || tid >= PER_ROW * R1Y) return;
-        const int c = tid / PER_ROW, m = tid - c * PER_ROW;
-        const int j = j0 - 1 + c;
-        const int a = 2 * m + ((c0 - (i0 - 1) - j - k) & 1);
-        const int i = i0 - 1 + a;
-        if (i < 1 || i > g.nx || j < 1 || j > g.ny) return;
-        SweepSlot<R>& S = slot(k);
-        S.x[c + 1][a + 3] = relax(S, slot(k - 1), slot(k + 1), c, a + 3, !ZERO);
-    };
-    // Second colour of plane k on the tile: thread t < 16*SY takes the m-th
+    constexpr int PF = R1X / 2;
+    const bool f_on = tid < PF * R1Y;
+    const int fc = f_on ? tid / PF : 0, fm = tid - fc * PF;
+    const int fj = j0 - 1 + fc;
+    const int fpar = (c0 - (i0 - 1) - fj) & 1;
+    const bool fj_ok = f_on && fj >= 1 && fj <= g.ny;
+    // Second colour of a plane on the tile: thread t < 16*SY takes the m-th
     // cell of that colour in tile row r; the values stay in shared memory.
-    auto second_colour = [&](int k) {
-        constexpr int PER_ROW = SX / 2;
-        if (tid >= PER_ROW * SY) return;
-        const int r = tid / PER_ROW, m = tid - r * PER_ROW;
-        const int j = j0 + r;
-        const int i = i0 + 2 * m + ((c0 + 1 - i0 - j - k) & 1);
-        if (i > g.nx || j > g.ny) return;
-        SweepSlot<R>& S = slot(k);
-        const int w = i - i0 + 4;
-        S.x[r + 2][w] = relax(S, slot(k - 1), slot(k + 1), r + 1, w, true);
+    constexpr int PS = SX / 2;
+    const bool s_on = tid < PS * SY;
+    const int sr = s_on ? tid / PS : 0, sm2 = tid - sr * PS;
+    const int sj = j0 + sr;
+    const int spar = (c0 + 1 - i0 - sj) & 1;
+    const bool sj_ok = s_on && sj <= g.ny;
+    // the coalesced store of a finished tile: one cell per thread
+    const bool w_on = i0 + tx <= g.nx && j0 + ty <= g.ny;
+    R* const wptr = xout + g.at(i0 + tx, j0 + ty, 0);
+
+    auto first_colour = [&](int k, SweepSlot<R>& S, const SweepSlot<R>& Sm, const SweepSlot<R>& Sp) {
+        if (!fj_ok || k < 1 || k > g.nz) return;
+        const int a = 2 * fm + ((fpar - k) & 1);
+        const int i = i0 - 1 + a;
+        if (i < 1 || i > g.nx) return;
+        S.x[fc + 1][a + 3] = relax(S, Sm, Sp, fc, a + 3, !ZERO);
     };
-    // Coalesced store of the finished tile of plane k (both colours).
-    auto write_out = [&](int k) {
-        const int i = i0 + tx, j = j0 + ty;
-        if (i > g.nx || j > g.ny) return;
-        const SweepSlot<R>& S = slot(k);
+    auto second_colour = [&](int k, SweepSlot<R>& S, const SweepSlot<R>& Sm, const SweepSlot<R>& Sp) {
+        if (!sj_ok) return;
+        const int i = i0 + 2 * sm2 + ((spar - k) & 1);
+        if (i > g.nx) return;
+        const int w = i - i0 + 4;
+        S.x[sr + 2][w] = relax(S, Sm, Sp, sr + 1, w, true);
+    };
+    auto write_out = [&](int k, const SweepSlot<R>& S) {
+        if (!w_on) return;
         const R v = S.x[ty + 2][tx + 4];
-        xout[g.at(i, j, k)] = v;
+        wptr[(long long)k * g.S] = v;
         if (dot) dacc += S.b[ty + 1][tx + 4] * v;
     };
 
@@ -613,23 +623,28 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     }
     for (int k = k0 - 2; k <= k0 + 1; ++k) correct(k);
     __syncthreads();
-    first_colour(k0 - 1);
+    first_colour(k0 - 1, slot(k0 - 1), slot(k0 - 2), slot(k0));
     __syncthreads();
-    first_colour(k0);
+    first_colour(k0, slot(k0), slot(k0 - 1), slot(k0 + 1));
+    int sk = slot_index(k0);                  // slot of plane k, advanced by one per plane
     for (int k = k0; k <= k1; ++k) {
+        const int skm1 = sk == 0 ? NSLOT - 1 : sk - 1;
+        const int skp1 = sk == NSLOT - 1 ? 0 : sk + 1;
+        const int skp2 = skp1 == NSLOT - 1 ? 0 : skp1 + 1;
         if (TMA) fence_proxy_async();         // this thread's generic accesses before the next copies
         issue(k + 4);                         // the slot of plane k-3, idle since k-2
         if (TMA) landed(k + 2);
         else cp_async_wait<2>();              // plane k+2 landed
         correct(k + 2);
         __syncthreads();
-        if (k > k0) write_out(k - 1);
-        first_colour(k + 1);
+        if (k > k0) write_out(k - 1, slots[skm1]);
+        first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
         __syncthreads();
-        second_colour(k);
+        second_colour(k, slots[sk], slots[skm1], slots[skp1]);
+        sk = skp1;
     }
     __syncthreads();
-    write_out(k1);
+    write_out(k1, slot(k1));
     if (TMA) {   // the copies still in flight land before the block exits
         landed(k1 + 3);
         landed(k1 + 4);
