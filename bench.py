@@ -70,6 +70,9 @@ def parse():
                     help="untimed steps before the warm-up: the timed window starts past "
                          "the start-up transient of the run (dt jump at step 3, first front "
                          "motion), as in the 500-2000-step runs the metric stands for")
+    ap.add_argument("--no-step-graph", action="store_true",
+                    help="host-driven steps (a read-back per PCG iteration) instead of one "
+                         "graph launch per step with the solver loops on the device")
     ap.add_argument("--warm-start", default="extrap", choices=["none", "extrap"],
                     help="start of each solve: previous pressure, or extrapolated in time")
     return ap.parse_args()
@@ -82,6 +85,7 @@ def solver_kwargs(args, solver=None):
     return dict(solver=solver or args.solver, rtol=args.rtol, w_from_level=args.w_from,
                 smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min,
                 graphs=not args.no_graphs, tma=not args.no_tma,
+                step_graph=not args.no_step_graph,
                 extrapolate=(not plain) and args.warm_start == "extrap")
 
 
@@ -225,10 +229,15 @@ def run_ours(args):
                      **solver_kwargs(args))
     L = sim.L
     KC_SMOOTH0 = 3
-    mask = (1 << len(KC_NAMES)) - 1 if args.breakdown else (1 << KC_SMOOTH0)
-    # the timing mask is part of the captured preconditioner graphs: set it
-    # before the warm-up so that the capture happens there, then reset the
-    # totals (same mask, no recapture) before the timed steps
+    NK = len(KC_NAMES)
+    # Kernel-class timers bracket every launch with events, and a step with
+    # timers on is host-driven (the device-resident step graph is off while
+    # they are): the timed steps run without them, except in a --breakdown run;
+    # the per-launch time of the roofline kernel comes from a second window of
+    # the same length right after, with its class timed.  The timing mask is
+    # part of the captured preconditioner graphs: it is set before the warm-up
+    # so that the capture happens there.
+    mask = (1 << NK) - 1 if args.breakdown else 0
     capi.check(L.wpf_set_kernel_timing(sim.h, mask), "timing")
     for _ in range(args.spinup + args.warmup):
         sim.step()
@@ -252,10 +261,16 @@ def run_ours(args):
     L.wpf_launch_count(sim.h, C.byref(n1))
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    NK = len(KC_NAMES)
     kms = (C.c_double * NK)()
     kcnt = (C.c_int64 * NK)()
+    if not args.breakdown:   # the roofline window: the finest-level smoother timed
+        capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
+        sim.step()   # recaptures the cycle graphs with the timer nodes
+        capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
+        for _ in range(args.steps):
+            sim.step()
     L.wpf_kernel_times(sim.h, kms, kcnt, NK)
+    capi.check(L.wpf_set_kernel_timing(sim.h, 0), "timing")
     t = torch.tensor([ms], device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)

@@ -101,6 +101,16 @@ typedef struct wpf_solver_opts {
 /* WPF_SOLVER_NO_TMA: stage the finest-level sweep with per-thread cp.async
  * copies instead of bulk-tensor (TMA) copies (same arithmetic, same results). */
 #define WPF_SOLVER_NO_TMA 4
+/* WPF_SOLVER_STEP_GRAPH: run wpf_step (from itime >= 3, once the extrapolated
+ * start holds two increments when WPF_SOLVER_EXTRAPOLATE is set) as one CUDA
+ * graph launch: the dt law, calcPermeability, the whole solve with its
+ * convergence tests on the device (conditional graph nodes: a WHILE node over
+ * the refinement passes holding a WHILE node over the PCG iterations) and the
+ * fused update, with one read-back per step.  The kernels, their order and so
+ * the results are those of the host-driven step.  wpf_ensemble_run then
+ * advances all such members in one launch of one graph.  Ignored while
+ * kernel timing is on or a warm-start net is attached.                     */
+#define WPF_SOLVER_STEP_GRAPH 8
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {
@@ -249,7 +259,10 @@ int wpf_snapshot_wait(wpf_handle* h);
  * kernels of some members fill the GPU while others wait on a read-back.
  * status[m] (may be NULL) gets each member's status; a member that failed
  * stops.  Returns WPF_OK, or the first failure other than
- * WPF_ERR_NOT_CONVERGED, else that.                                         */
+ * WPF_ERR_NOT_CONVERGED, else that.  A step in which every member can take
+ * the device-resident step (WPF_SOLVER_STEP_GRAPH) is instead one launch of
+ * one graph holding all members' steps as independent branches, followed by
+ * one synchronisation; the graphs are cached per buffer assignment.        */
 int wpf_ensemble_run(wpf_handle** members, int32_t n, int32_t itime0, int32_t nsteps, int32_t nthreads,
                      double* dtime, wpf_step_stats* stats, int32_t* status);
 

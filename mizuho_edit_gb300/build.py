@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["wpf_capi.cu", "wpf_physics.cu", "wpf_solver.cu", "wpf_noalloc.cu", "wpf_net.cu",
-           "wpf_ensemble.cu"]
+           "wpf_ensemble.cu", "wpf_graph.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

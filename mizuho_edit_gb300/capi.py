@@ -27,6 +27,7 @@ SOLVER_MIXED = 1
 SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bits
 SOLVER_EXTRAPOLATE = 2
 SOLVER_NO_TMA = 4
+SOLVER_STEP_GRAPH = 8
 
 
 class WpfError(RuntimeError):

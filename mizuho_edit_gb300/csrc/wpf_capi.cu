@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <vector>
 
 #include "wpf_internal.cuh"
@@ -116,6 +117,10 @@ static Phys make_phys(const wpf_params& p) {
 }
 
 static void free_all(wpf_handle* h) {
+    step_graphs_drop(h);
+    if (h->gctl) cudaFree(h->gctl);
+    if (h->gctl_host) cudaFreeHost(h->gctl_host);
+    if (h->gdsc_host) cudaFreeHost(h->gdsc_host);
     double* d[] = {h->krock, h->phase, h->concent, h->pressure, h->phase_n, h->concent_n,
                    h->T[0], h->T[1], h->T[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
                    h->vel[0], h->vel[1], h->vel[2], h->dphasedt, h->dconcentdt, h->dir_val,
@@ -172,6 +177,8 @@ int wpf_create(const wpf_params* p, wpf_handle** out) {
     if (!h) return WPF_ERR_NOMEM;
     new (&h->h64) Hierarchy<double>();
     new (&h->h32) Hierarchy<float>();
+    static std::atomic<unsigned long long> next_uid{1};
+    h->uid = next_uid++;
     h->prm = *p;
     h->phys = make_phys(*p);
     h->g = make_grid(p->nx, p->ny, p->nz);
@@ -308,6 +315,7 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
     WPF_CUDA(cudaStreamSynchronize(h->stream));   // host vectors go out of scope
     h->have_wells = true;
     h->ws_hist = 0;   // new boundary conditions: the increment history no longer applies
+    step_graphs_drop(h);   // the step graphs bake in the well arrays
     return phys_set_dirichlet(h);
 }
 
@@ -509,6 +517,10 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     wpf_step_stats tmp;
     memset(&tmp, 0, sizeof(tmp));
     wpf_step_stats* s = st ? st : &tmp;
+    if (step_graph_ready(h, itime)) {   // the whole step as one graph launch
+        memset(s, 0, sizeof(*s));
+        return step_graph_run(h, s, dtime_inout);
+    }
     const long long l0 = h->nlaunch;
     int rc = phys_permeability(h, false);
     if (rc) return rc;

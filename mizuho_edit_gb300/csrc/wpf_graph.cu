@@ -1,0 +1,328 @@
+// wpf_graph.cu -- the device-resident step (WPF_SOLVER_STEP_GRAPH).
+//
+// wpf_step's host-driven form (wPFAW3D.f90:2227-2280: dt law,
+// calcPermeability, solvePressure, the fused velocity/phase/concentration
+// update) reads a scalar back after every residual and every PCG iteration to
+// decide what to launch next.  Here the whole step is one CUDA graph: the dt
+// law and the solver's decisions run in one-thread control kernels, the two
+// solver loops are conditional WHILE nodes whose handles those kernels set,
+// and the step ends with two device-to-host copies (the control block and the
+// scalar slots) read after the one synchronisation of the step.  The kernels
+// and their order are those of the host-driven step, so are the results.
+//
+// A graph bakes in the buffers it was captured with; the step's ping-pong
+// buffers (phase, concentration and, with the extrapolated start, the three
+// increment buffers) cycle with period 6, so a handle keeps instantiated
+// graphs keyed by the assignment of those buffers (and by whether the face
+// transmissibilities can be updated from the last step's phase, which a
+// wpf_upload of the phase rules out: up to 12 graphs).
+#include <math.h>
+#include <string.h>
+
+#include "wpf_internal.cuh"
+
+namespace wpf {
+
+// ---- graph building ----------------------------------------------------------
+int gb_begin(GraphBuilder& b) {
+    WPF_CUDA(cudaStreamBeginCaptureToGraph(b.s, b.graph, b.ndeps ? b.deps : nullptr, nullptr, (size_t)b.ndeps,
+                                           cudaStreamCaptureModeThreadLocal));
+    b.capturing = true;
+    return WPF_OK;
+}
+
+int gb_end(GraphBuilder& b) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    const cudaError_t e1 = cudaStreamGetCaptureInfo(b.s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    const bool fits = e1 == cudaSuccess && nd <= 8;
+    if (fits) {
+        for (size_t q = 0; q < nd; ++q) b.deps[q] = deps[q];
+        b.ndeps = (int)nd;
+    }
+    cudaGraph_t out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(b.s, &out);
+    b.capturing = false;
+    if (!fits || e2 != cudaSuccess || cs != cudaStreamCaptureStatusActive) {
+        cudaGetLastError();
+        return WPF_ERR_CUDA;
+    }
+    return WPF_OK;
+}
+
+int gb_handle(GraphBuilder& b, cudaGraphConditionalHandle* hd) {
+    WPF_CUDA(cudaGraphConditionalHandleCreate(hd, b.top, 0, cudaGraphCondAssignDefault));
+    return WPF_OK;
+}
+
+int gb_cond(GraphBuilder& b, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hd,
+            GraphBuilder* body) {
+    // (the parameter union has no default constructor: zeroed raw storage)
+    alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+    memset(raw, 0, sizeof(raw));
+    cudaGraphNodeParams& p = *reinterpret_cast<cudaGraphNodeParams*>(raw);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = hd;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    WPF_CUDA(cudaGraphAddNode(&node, b.graph, b.ndeps ? b.deps : nullptr, nullptr, (size_t)b.ndeps, &p));
+    body->graph = p.conditional.phGraph_out[0];
+    body->top = b.top;
+    body->s = b.s;
+    body->ndeps = 0;
+    body->capturing = false;
+    b.deps[0] = node;
+    b.ndeps = 1;
+    return WPF_OK;
+}
+
+// ---- step control kernels ------------------------------------------------------
+// The dt law of wPFAW3D.f90:2227-2230, dt = dt_c * min(dt_a, taumin), with
+// dt_c = tfac * dx^2 / (2 eps^2) and dt_a = eps^2 / D, taumin from the key the
+// previous update left in S_TAUMIN_KEY; the extrapolation coefficients of
+// ws_coeffs for two held increments; the solve's control state and slots reset.
+__global__ void k_step_begin(StepCtl* c, double* dsc, double dt_c, double dt_a) {
+    if (threadIdx.x) return;
+    const double tm = dkey_inv(reinterpret_cast<const unsigned long long*>(dsc)[S_TAUMIN_KEY]);
+    const double dt = dt_c * (dt_a < tm ? dt_a : tm);
+    c->dt = dt;
+    const double hn = dt, h1 = c->h1, h2 = c->h2;
+    if (!(hn > 0 && h1 > 0 && h2 > 0)) {
+        c->wa = 2.f;
+        c->wb = -1.f;
+    } else {
+        const double q = hn * (hn + h1) / (h1 + h2);
+        c->wa = (float)(hn / h1 + q / h1);
+        c->wb = (float)(-q / h2);
+    }
+    c->bnorm = c->relres = c->relres0 = c->r0 = c->tol = 0.0;
+    c->pass = c->outer = c->inner = c->it = c->need_pcg = c->accept = c->used = c->pcgs = 0;
+    c->status = WPF_ERR_NOT_CONVERGED;
+    for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;   // RR64 BB64 RR0WS RW WW
+    dsc[S_WSS2] = 0.0;
+    dsc[S_WSD2] = 0.0;
+}
+
+// A converged solve's increment becomes the newest of the history.
+__global__ void k_step_end(StepCtl* c) {
+    if (threadIdx.x) return;
+    if (c->status == WPF_OK) {
+        c->h2 = c->h1;
+        c->h1 = c->dt;
+    }
+}
+
+// ---- host side ------------------------------------------------------------------
+static bool ws_enabled(const wpf_handle* h) { return (h->opts.flags & WPF_SOLVER_EXTRAPOLATE) != 0; }
+
+bool step_graph_ready(const wpf_handle* h, int itime) {
+    const int f = h->opts.flags;
+    return (f & WPF_SOLVER_STEP_GRAPH) && !(f & WPF_SOLVER_NO_GRAPHS) && itime >= 3 && h->timing_mask == 0 &&
+           !h->ws_net && h->opts.max_outer >= 1 && h->have_wells && h->ndir > 0 &&
+           (!ws_enabled(h) || h->ws_hist == 2);
+}
+
+int step_graph_prepare(wpf_handle* h) {
+    int rc = solver_setup(h);
+    if (rc) return rc;
+    const Grid& g = h->g;
+    if (!h->work && (rc = dev_alloc(h, (void**)&h->work, sizeof(int) * (size_t)g.nx * g.ny * g.nz))) return rc;
+    if (ws_enabled(h) && !h->ws_e[0] && (rc = dev_alloc(h, (void**)&h->ws_e[0], sizeof(float) * g.total)))
+        return rc;
+    if (!h->gctl) {
+        if ((rc = dev_alloc(h, (void**)&h->gctl, sizeof(StepCtl)))) return rc;
+        WPF_CUDA(cudaMallocHost((void**)&h->gctl_host, sizeof(StepCtl)));
+        memset(h->gctl_host, 0, sizeof(StepCtl));
+        WPF_CUDA(cudaMallocHost((void**)&h->gdsc_host, S_COUNT * sizeof(double)));
+        h->gctl_dirty = true;
+    }
+    return WPF_OK;
+}
+
+// Capture one step of h into b (b not capturing on entry or exit).  The
+// capture-time calls are launches only; the host flags phys_permeability
+// sets are restored, since the graph runs later.
+int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
+    cudaStream_t s = h->stream;
+    const wpf_params& p = h->prm;
+    const double e2 = p.epsilon * p.epsilon;
+    const double dt_c = p.tfac * 0.5 * (p.dx * p.dx) / e2;
+    const double dt_a = e2 / p.diffusion;
+    StepCtl* c = h->gctl;
+    int rc;
+    if ((rc = gb_begin(b))) return rc;
+    long long l0 = h->nlaunch;
+    WPF_LAUNCH(h, KC_OTHER, k_step_begin<<<1, 32, 0, s>>>(c, h->dsc, dt_c, dt_a));
+    const bool tc = h->t_current, tp = h->t_from_prev, kv = h->kf_valid;
+    rc = phys_permeability(h, false);
+    h->t_current = tc;
+    h->t_from_prev = tp;
+    h->kf_valid = kv;
+    if (rc) return rc;
+    n->fixed += h->nlaunch - l0;
+    if ((rc = solve_capture(h, b, n))) return rc;
+    l0 = h->nlaunch;
+    if ((rc = phys_capture_update(h, &c->dt))) return rc;
+    WPF_LAUNCH(h, KC_OTHER, k_step_end<<<1, 32, 0, s>>>(c));
+    WPF_CUDA(cudaGetLastError());
+    WPF_CUDA(cudaMemcpyAsync(h->gctl_host, c, sizeof(StepCtl), cudaMemcpyDeviceToHost, s));
+    WPF_CUDA(cudaMemcpyAsync(h->gdsc_host, h->dsc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+    n->fixed += h->nlaunch - l0;
+    return gb_end(b);
+}
+
+// End a capture left open by a failure, so that the stream is usable again.
+void abandon_capture(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t t = nullptr;
+        cudaStreamEndCapture(s, &t);
+    }
+    cudaGetLastError();
+}
+
+// Host state after a device-resident step, as the host-driven step leaves it.
+int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, double* dt_out) {
+    const StepCtl c = *h->gctl_host;
+    const double* d = h->gdsc_host;
+    unsigned long long key, ov, um;
+    memcpy(&key, d + S_TAUMIN_KEY, 8);
+    memcpy(&ov, d + S_OVERSHOOT, 8);
+    memcpy(&um, d + S_UMAX_BITS, 8);
+    double umax;
+    memcpy(&umax, &um, 8);
+    int nw[2], kerr = 0;
+    memcpy(nw, d + S_NWORK, sizeof(nw));
+    memcpy(&kerr, d + S_KERR, sizeof(int));
+    const double taumin = dkey_inv(key);
+    h->taumin_last = taumin;
+    h->last_active = nw[0] + nw[1];
+    h->ws_hn = c.dt;
+    h->ws_used = c.used;
+    if (c.used < 0) ++h->ws_fallbacks;
+    if (ws_enabled(h) && h->ws[0]) {
+        if (c.status == WPF_OK) {
+            float* t = h->ws[1];
+            h->ws[1] = h->ws[0];
+            h->ws[0] = h->ws[2];
+            h->ws[2] = t;
+            h->ws_hist = h->ws_hist < 2 ? h->ws_hist + 1 : 2;
+            h->ws_h2 = h->ws_h1;
+            h->ws_h1 = c.dt;
+        } else {
+            h->ws_hist = 0;
+        }
+    }
+    double* t = h->phase; h->phase = h->phase_n; h->phase_n = t;
+    t = h->concent; h->concent = h->concent_n; h->concent_n = t;
+    h->vel_valid = false;
+    h->kf_valid = false;
+    h->t_from_prev = true;   // T came from the phase now in phase_n
+    h->t_current = false;
+    const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter;
+    h->nlaunch += launches;
+    int rc = c.status;
+    if (kerr) {   // a sweep whose bounded staging wait ran out left its flag
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KERR, 0, sizeof(double), h->stream));
+        WPF_CUDA(cudaStreamSynchronize(h->stream));
+        rc = WPF_ERR_TIMEOUT;
+    }
+    if (st) {
+        st->outer_iterations = c.outer;
+        st->inner_iterations = c.inner;
+        st->converged = c.status == WPF_OK;
+        st->relres = c.relres;
+        st->relres0 = c.relres0;
+        st->warm_start = c.used;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+        st->solve_ms = ms;
+        ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+        st->update_ms = ms;
+        st->taumin = taumin;
+        st->overshoot_cells = (int32_t)ov;
+        st->dtime = c.dt;
+        st->max_courant = umax * c.dt / h->prm.dx;
+        st->kernel_launches = (int32_t)launches;
+    }
+    cudaGetLastError();
+    if (dt_out) *dt_out = c.dt;
+    return rc;
+}
+
+void step_graph_key(const wpf_handle* h, const void** k) {
+    const bool ws = ws_enabled(h);
+    k[0] = h->phase;
+    k[1] = h->concent;
+    k[2] = ws ? h->ws[0] : nullptr;
+    k[3] = ws ? h->ws[1] : nullptr;
+    k[4] = ws ? h->ws[2] : nullptr;
+    // calcPermeability recomputes only the faces whose cells changed phase when
+    // T came from the phase now in phase_n (the last step), else every face
+    k[5] = h->t_from_prev ? h->phase_n : nullptr;
+}
+
+// Upload the increment step sizes when the host-driven path changed them.
+int step_graph_sync_ctl(wpf_handle* h) {
+    if (!h->gctl_dirty) return WPF_OK;
+    h->gctl_host->h1 = h->ws_h1;
+    h->gctl_host->h2 = h->ws_h2;
+    WPF_CUDA(cudaMemcpyAsync(h->gctl, h->gctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+    h->gctl_dirty = false;
+    return WPF_OK;
+}
+
+int step_graph_run(wpf_handle* h, wpf_step_stats* st, double* dt_out) {
+    int rc = step_graph_prepare(h);
+    if (rc) return rc;
+    const void* key[6];
+    step_graph_key(h, key);
+    int slot = -1;
+    for (int q = 0; q < h->nsg; ++q)
+        if (!memcmp(h->sg[q].key, key, sizeof(key))) slot = q;
+    if (slot < 0) {
+        if (h->nsg == wpf_handle::MAX_STEP_GRAPHS) {   // drop the oldest
+            cudaGraphExecDestroy(h->sg[0].exec);
+            memmove(&h->sg[0], &h->sg[1], sizeof(h->sg[0]) * (wpf_handle::MAX_STEP_GRAPHS - 1));
+            --h->nsg;
+        }
+        GraphBuilder b;
+        WPF_CUDA(cudaGraphCreate(&b.graph, 0));
+        b.top = b.graph;
+        b.s = h->stream;
+        StepCounts n;
+        const long long saved = h->nlaunch;
+        rc = step_graph_capture(h, b, &n);
+        h->nlaunch = saved;
+        if (b.capturing || rc) abandon_capture(h->stream);
+        cudaGraphExec_t exec = nullptr;
+        if (!rc && cudaGraphInstantiate(&exec, b.graph, 0) != cudaSuccess) {
+            cudaGetLastError();
+            rc = WPF_ERR_CUDA;
+        }
+        cudaGraphDestroy(b.graph);
+        if (rc) return rc;
+        slot = h->nsg++;
+        memcpy(h->sg[slot].key, key, sizeof(key));
+        h->sg[slot].exec = exec;
+        h->sg[slot].n = n;
+    }
+    if ((rc = step_graph_sync_ctl(h))) return rc;
+    WPF_CUDA(cudaGraphLaunch(h->sg[slot].exec, h->stream));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return step_graph_finish(h, h->sg[slot].n, st, dt_out);
+}
+
+void step_graphs_drop(wpf_handle* h) {
+    for (int q = 0; q < h->nsg; ++q)
+        if (h->sg[q].exec) cudaGraphExecDestroy(h->sg[q].exec);
+    h->nsg = 0;
+    ++h->epoch;
+    h->gctl_dirty = true;
+    ensemble_graphs_forget(h);
+}
+
+}  // namespace wpf

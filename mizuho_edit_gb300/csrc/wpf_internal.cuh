@@ -96,6 +96,53 @@ struct SweepMaps {
     CUtensorMap x, cx, cy, cz, id, b;
 };
 
+// Control block of the device-resident step (WPF_SOLVER_STEP_GRAPH): the
+// decisions the host-driven step takes after each read-back, taken instead by
+// one-thread kernels inside the step graph.  Copied back once per step.
+struct StepCtl {
+    double dt;               // this step's dt (the dt law on the device)
+    double h1, h2;           // step sizes of the last two increments
+    float wa, wb;            // extrapolation coefficients e = wa d1 + wb d2
+    double bnorm, relres, relres0;
+    double r0, tol;          // PCG: ||r_0|| and the relative tolerance of this pass
+    int pass;                // refinement pass whose residual was taken last
+    int outer, inner;        // refinement passes with a PCG, PCG iterations in all
+    int it;                  // iterations of the current PCG
+    int need_pcg;            // this pass runs a PCG (else it adds the accepted start only)
+    int accept;              // extrapolated start accepted, not yet added to p
+    int used;                // 1 start used, -1 rejected, 0 not tried
+    int status;              // WPF_OK / WPF_ERR_NOT_CONVERGED / WPF_ERR_NONFINITE
+    int pcgs;                // PCG runs
+    int pad;
+};
+
+// Builds a CUDA graph from stream-captured segments and conditional nodes.
+// `graph` is the graph being extended (the top graph or a conditional body),
+// `deps` the nodes the next segment depends on.
+struct GraphBuilder {
+    cudaGraph_t graph = nullptr;
+    cudaGraph_t top = nullptr;    // owner of the conditional handles
+    cudaStream_t s = nullptr;
+    cudaGraphNode_t deps[8];
+    int ndeps = 0;
+    bool capturing = false;
+};
+int gb_begin(GraphBuilder& b);   // capture s into graph after deps
+int gb_end(GraphBuilder& b);     // end the capture; deps = its leaves
+// A conditional handle on the top graph (reset to 0 at each launch); the
+// kernels that set it take it as an argument, so it exists before their capture.
+int gb_handle(GraphBuilder& b, cudaGraphConditionalHandle* hd);
+// Append a conditional node (WHILE or IF) on handle hd after deps; `body` is
+// set up to build its body graph.
+int gb_cond(GraphBuilder& b, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hd,
+            GraphBuilder* body);
+
+// Kernels launched per step by a captured device-resident step:
+//   fixed + passes * per_pass + iterations * per_iter.
+struct StepCounts {
+    long long fixed = 0, per_pass = 0, per_iter = 0;
+};
+
 template <typename R>
 struct Hierarchy {
     int nlev = 0;
@@ -195,6 +242,22 @@ struct wpf_handle {
     int ngpend;
     int gpend_cls[512];
     cudaEvent_t gpend_a[512], gpend_b[512];
+    // device-resident step: control block (device, pinned mirror), pinned
+    // copy of the scalar slots, and the instantiated step graphs, one per
+    // assignment of the ping-pong buffers (phase, concentration, increments)
+    wpf::StepCtl* gctl;
+    wpf::StepCtl* gctl_host;
+    double* gdsc_host;
+    bool gctl_dirty;         // the host-driven path ran since the last graph step
+    static constexpr int MAX_STEP_GRAPHS = 12;
+    struct StepGraph {
+        const void* key[6];
+        cudaGraphExec_t exec;
+        wpf::StepCounts n;
+    } sg[MAX_STEP_GRAPHS];
+    int nsg;
+    unsigned long long uid;  // unique per handle over the process (ensemble graph keys)
+    unsigned long long epoch;   // bumped whenever captured graphs become invalid
 };
 
 namespace wpf {
@@ -383,6 +446,22 @@ int ws_net_correction(wpf_handle* h);                   // ws_e[1] from the atta
 
 int ensure_per_routine_arrays(wpf_handle* h);
 int dev_alloc(wpf_handle* h, void** p, size_t bytes);
+
+// device-resident step (wpf_graph.cu, wpf_solver.cu, wpf_physics.cu)
+// capture the solve (Dirichlet values .. pressure halo) into b, in capture on entry and exit
+int solve_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
+// capture the fused update with dt read from *dtp (launches only, no host state change)
+int phys_capture_update(wpf_handle* h, const double* dtp);
+bool step_graph_ready(const wpf_handle* h, int itime);
+int step_graph_prepare(wpf_handle* h);           // allocations a capture needs
+int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
+int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, double* dt_out);
+int step_graph_run(wpf_handle* h, wpf_step_stats* st, double* dt_out);
+void step_graph_key(const wpf_handle* h, const void** k);   // STEP_KEY buffer pointers
+int step_graph_sync_ctl(wpf_handle* h);          // upload host-side history if stale
+void step_graphs_drop(wpf_handle* h);
+void abandon_capture(cudaStream_t s);
+void ensemble_graphs_forget(const wpf_handle* h);   // wpf_ensemble.cu
 
 inline dim3 cell_block() { return dim3(32, 4, 2); }
 inline dim3 cell_grid(int nx, int ny, int nz) {

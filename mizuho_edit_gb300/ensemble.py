@@ -1,9 +1,13 @@
 """Ensembles of permeability realisations with uneven grids, advanced together.
 
 The members are independent wPFAW3D domains (no counterpart in the reference,
-which runs one).  ``wpf_ensemble_run`` steps them from a pool of host threads,
-each member on its own stream, so that small grids -- whose kernels are too
-short to fill 152 SMs -- overlap on the device.  Before the timed run, an
+which runs one).  ``wpf_ensemble_run`` advances them together: once every
+member can take the device-resident step, each ensemble step is one launch of
+one CUDA graph holding all members' steps as independent branches (their
+solver loops are conditional nodes), so that small grids -- whose kernels are
+too short to fill 152 SMs -- overlap on the device with no host round trip;
+before that (the first steps) a pool of host threads steps the members, each
+on its own stream.  Before the timed run, an
 autotuner picks, per grid shape, the solver configuration (multigrid cycle
 shape, the level size from which the pipelined sweep kernel is used,
 smoothing sweeps) with the best measured time per step.
@@ -48,10 +52,10 @@ def _opts(c):
     return dict(w_from_level=w, sweep_min_cells=thr, smooth_sweeps=nu)
 
 
-def _sim(shape, kw, opts):
+def _sim(shape, kw, opts, step_graph=False):
     case = make_case(shape, **kw)
     return Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed", rtol=1e-8,
-                      extrapolate=True, **opts)
+                      extrapolate=True, step_graph=step_graph, **opts)
 
 
 def autotune(members, spinup: int = 20, steps: int = 6, log=print):
@@ -83,11 +87,14 @@ def autotune(members, spinup: int = 20, steps: int = 6, log=print):
     return best
 
 
-def run(members, tuned, steps: int, spinup: int, threads: int, log=print):
+def run(members, tuned, steps: int, spinup: int, threads: int, log=print, step_graph: bool = True):
     """Advance every member `spinup` untimed steps, then `steps` timed ones
-    through wpf_ensemble_run; returns the throughput figures."""
+    through wpf_ensemble_run (step_graph: every step from the third one launch
+    of one graph holding all members; else host-driven steps from a thread
+    pool); returns the throughput figures."""
     import torch
-    sims = [_sim(shape, kw, _opts(tuned[shape][0] if tuned else CANDIDATES[0])) for shape, kw in members]
+    sims = [_sim(shape, kw, _opts(tuned[shape][0] if tuned else CANDIDATES[0]), step_graph)
+            for shape, kw in members]
     try:
         L = sims[0].L
         n = len(sims)
@@ -105,6 +112,7 @@ def run(members, tuned, steps: int, spinup: int, threads: int, log=print):
         cells = sum(int(np.prod(shape)) for shape, _ in members)
         res = {"members": n, "shapes": {str(s): sum(1 for m in members if m[0] == s) for s in SHAPES},
                "steps": steps, "spinup": spinup, "threads": threads, "wall_s": wall,
+               "one_graph_per_step": step_graph,
                "ensemble_cell_updates_per_s": cells * steps / wall,
                "member_steps_per_s": n * steps / wall,
                "converged_last_step": int(sum(1 for s in stats if s.converged)),
@@ -122,18 +130,23 @@ def main(argv=None):
     ap.add_argument("--spinup", type=int, default=20)
     ap.add_argument("--threads", type=int, default=16)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--host-steps", action="store_true",
+                    help="host-driven steps only (no device-resident step graphs)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     counts = tuple(int(x) for x in a.members.split(","))
     members = make_members(counts)
     tuned = None if a.no_tune else autotune(members)
-    res = run(members, tuned, a.steps, a.spinup, a.threads)
+    res = run(members, tuned, a.steps, a.spinup, a.threads, step_graph=not a.host_steps)
+    if not a.host_steps:   # the thread-pool form on the same members, for comparison
+        res["host_threaded_cell_updates_per_s"] = run(
+            members, tuned, a.steps, a.spinup, a.threads, step_graph=False)["ensemble_cell_updates_per_s"]
     res["tuned"] = ({str(k): {"w_from_level": v[0][0], "sweep_min_cells": v[0][1], "smooth_sweeps": v[0][2],
                               "ms_per_step": {str(c): t for c, t in v[1].items()}}
                      for k, v in tuned.items()} if tuned else None)
     # the same members one after the other on one thread, for comparison
     if not a.no_tune:
-        seq = run(members, tuned, max(a.steps // 4, 2), a.spinup, 1)
+        seq = run(members, tuned, max(a.steps // 4, 2), a.spinup, 1, step_graph=False)
         res["one_thread_cell_updates_per_s"] = seq["ensemble_cell_updates_per_s"]
     s = json.dumps(res)
     print(s)

@@ -1,0 +1,177 @@
+"""The device-resident step (WPF_SOLVER_STEP_GRAPH): each step from the
+fourth is one CUDA graph launch with the dt law and the solver's two loops on
+the device (conditional WHILE nodes set by one-thread control kernels).  It
+launches the same field kernels in the same order as the host-driven step, so
+iteration counts and warm-start decisions must be equal and fields, dt and
+residuals equal up to the run-to-run rounding of the atomically accumulated dot
+products (two host-driven runs differ by as much), for one domain and for an
+ensemble advanced in one launch of one graph."""
+import ctypes as C
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("phase", "concent", "pressure")
+SAME = ("outer_iterations", "inner_iterations", "converged", "warm_start", "overshoot_cells")
+CLOSE = ("dtime", "taumin")
+TOL_FIELD = 1e-11   # relative L2
+TOL_SCALAR = 1e-9   # relative
+# the residuals are ||r|| / ||b||: rounding noise of p moves them by ~1e-16 absolute
+RESID = ("relres", "relres0")
+TOL_RESID = 1e-13   # absolute
+
+
+def _close(a, b, tol):
+    return abs(a - b) <= tol * max(abs(a), abs(b), 1e-300)
+
+
+def _same_stats(a, b, where):
+    for key in SAME:
+        assert a[key] == b[key], (where, key, a[key], b[key])
+    for key in CLOSE:
+        assert _close(a[key], b[key], TOL_SCALAR), (where, key, a[key], b[key])
+    for key in RESID:
+        assert abs(a[key] - b[key]) <= TOL_RESID, (where, key, a[key], b[key])
+
+
+def _same_fields(f0, f1):
+    from conftest import rel_l2
+    for k in FIELDS:
+        assert rel_l2(f1[k], f0[k]) <= TOL_FIELD, k
+
+
+def _case(shape=(40, 32, 24), seed=4, **kw):
+    from mizuho_edit_gb300.cases import make_case
+    kw = {**dict(log_var=2.0, corr_len=5.0, da=20.0), **kw}
+    return make_case(shape, seed=seed, **kw)
+
+
+def _sim(case, **kw):
+    from mizuho_edit_gb300.sim import Simulation
+    return Simulation(case.params, case.permeab_rock, case.phase, case.concent, **kw)
+
+
+def _run(case, nsteps, allow_unconverged=False, between=None, **kw):
+    with _sim(case, **kw) as sim:
+        stats = []
+        for s in range(nsteps):
+            if between and s in between:
+                between[s](sim)
+            stats.append(sim.step(allow_unconverged=allow_unconverged).as_dict())
+        return stats, sim.download(*FIELDS)
+
+
+def _assert_same(host, graph, first_graph_step=2):
+    (s0, f0), (s1, f1) = host, graph
+    _same_fields(f0, f1)
+    for n, (a, b) in enumerate(zip(s0, s1)):
+        _same_stats(a, b, n)
+    # the graph form really ran: its step adds control kernels
+    assert all(a["kernel_launches"] != b["kernel_launches"] for a, b in zip(s0[first_graph_step:],
+                                                                          s1[first_graph_step:]))
+
+
+@pytest.mark.parametrize("solver,extrapolate", [("mixed", True), ("fp64", False), ("mixed", False),
+                                                ("fp64", True)])
+def test_step_graph_matches_host_driven(solver, extrapolate):
+    case = _case()
+    kw = dict(solver=solver, rtol=1e-8, extrapolate=extrapolate)
+    _assert_same(_run(case, 12, **kw), _run(case, 12, step_graph=True, **kw))
+
+
+def test_step_graph_pipelined_levels():
+    """The two finest levels on the pipelined (TMA-staged) sweep inside the graph."""
+    case = _case((64, 64, 48), seed=9, log_var=1.5, corr_len=8.0)
+    kw = dict(solver="mixed", rtol=1e-8, extrapolate=True, sweep_min_cells=1 << 14)
+    _assert_same(_run(case, 7, **kw), _run(case, 7, step_graph=True, **kw))
+
+
+def test_step_graph_after_upload_matches():
+    """A host round trip of the fields between steps: wpf_upload of the phase
+    rules out the incremental permeability update, so the next step takes the
+    graph captured with every face recomputed, as the host-driven step does."""
+    case = _case(seed=11)
+    kw = dict(solver="mixed", rtol=1e-8, extrapolate=True)
+
+    def roundtrip(sim):
+        f = sim.download(*FIELDS)
+        sim.upload(None, f["phase"], f["concent"], f["pressure"])
+
+    between = {s: roundtrip for s in (4, 5, 8)}
+    _assert_same(_run(case, 10, between=between, **kw),
+                 _run(case, 10, between=between, step_graph=True, **kw))
+
+
+def test_step_graph_rebuilt_after_solver_change():
+    """New solver options drop the captured steps; the next graph step is
+    recaptured with them (the history restarts as in the host-driven form)."""
+    case = _case(seed=6)
+    kw = dict(solver="mixed", rtol=1e-8, extrapolate=True)
+    change = {6: lambda sim: sim.set_solver("mixed", 1e-8, extrapolate=True, smooth_sweeps=3,
+                                            step_graph=sim._sg)}
+
+    def run(sg):
+        with _sim(case, step_graph=sg, **kw) as sim:
+            sim._sg = sg
+            stats = []
+            for s in range(12):
+                if s in change:
+                    change[s](sim)
+                stats.append(sim.step().as_dict())
+            return stats, sim.download(*FIELDS)
+
+    host, graph = run(False), run(True)
+    _same_fields(host[1], graph[1])
+    for n, (a, b) in enumerate(zip(host[0], graph[0])):
+        _same_stats(a, b, n)
+
+
+def test_step_graph_not_converged_matches():
+    """A PCG capped at two iterations and two refinement passes: the solve
+    stops unconverged in both forms with the same fields and counts."""
+    case = _case(seed=8)
+    kw = dict(solver="fp64", rtol=1e-12, max_inner=2, max_outer=2)
+    host = _run(case, 6, allow_unconverged=True, **kw)
+    graph = _run(case, 6, allow_unconverged=True, step_graph=True, **kw)
+    assert not any(s["converged"] for s in host[0][2:])
+    _assert_same(host, graph)
+
+
+def test_ensemble_one_graph_matches_members_alone():
+    from mizuho_edit_gb300 import capi, ensemble
+    members = [((24, 20, 16), dict(log_var=1.0, corr_len=4.0, da=5.0, seed=1)),
+               ((32, 32, 32), dict(log_var=2.0, corr_len=6.0, da=30.0, seed=2)),
+               ((48, 40, 36), dict(log_var=0.5, corr_len=3.0, da=1.0, seed=3))]
+    opts = ensemble._opts(ensemble.CANDIDATES[0])
+    nsteps = 9
+    alone = []
+    for shape, kw in members:   # host-driven, one at a time
+        with ensemble._sim(shape, kw, opts) as sim:
+            stats = [sim.step().as_dict() for _ in range(nsteps)]
+            alone.append((stats, sim.download(*FIELDS)))
+    sims = [ensemble._sim(shape, kw, opts) for shape, kw in members]
+    try:
+        for s in sims:
+            s.set_solver("mixed", 1e-8, extrapolate=True, step_graph=True, **opts)
+        L = sims[0].L
+        n = len(sims)
+        hs = (C.c_void_p * n)(*[s.h.value for s in sims])
+        dt = (C.c_double * n)(*[s.dtime for s in sims])
+        stats = (capi.StepStats * n)()
+        status = (C.c_int32 * n)()
+        # steps 1-2 through the thread pool, from step 3 one graph launch per step
+        capi.check(L.wpf_ensemble_run(hs, n, 1, 3, 2, dt, stats, status), "wpf_ensemble_run")
+        for t in range(4, nsteps + 1):
+            capi.check(L.wpf_ensemble_run(hs, n, t, 1, 2, dt, stats, status), "wpf_ensemble_run")
+            assert list(status) == [0] * n
+            for m in range(n):
+                ref = alone[m][0][t - 1]
+                got = stats[m].as_dict()
+                _same_stats(ref, got, (m, t))
+                assert got["kernel_launches"] != ref["kernel_launches"]
+        for s, (_, ref) in zip(sims, alone):
+            _same_fields(ref, s.download(*FIELDS))
+    finally:
+        for s in sims:
+            s.close()
