@@ -121,6 +121,9 @@ static void free_all(wpf_handle* h) {
     if (h->gctl) cudaFree(h->gctl);
     if (h->gctl_host) cudaFreeHost(h->gctl_host);
     if (h->gdsc_host) cudaFreeHost(h->gdsc_host);
+    if (h->cap_side) cudaStreamDestroy(h->cap_side);
+    if (h->cap_fork) cudaEventDestroy(h->cap_fork);
+    if (h->cap_join) cudaEventDestroy(h->cap_join);
     double* d[] = {h->krock, h->phase, h->concent, h->pressure, h->phase_n, h->concent_n,
                    h->T[0], h->T[1], h->T[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
                    h->vel[0], h->vel[1], h->vel[2], h->dphasedt, h->dconcentdt, h->dir_val,

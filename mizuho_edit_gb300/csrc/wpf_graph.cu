@@ -78,6 +78,20 @@ int gb_cond(GraphBuilder& b, cudaGraphConditionalNodeType type, cudaGraphConditi
     return WPF_OK;
 }
 
+// A second stream forks from / joins the capture on h->stream (dependency
+// edges only: the events are recorded without the external flag).
+int gb_fork(wpf_handle* h) {
+    WPF_CUDA(cudaEventRecord(h->cap_fork, h->stream));
+    WPF_CUDA(cudaStreamWaitEvent(h->cap_side, h->cap_fork, 0));
+    return WPF_OK;
+}
+
+int gb_join(wpf_handle* h) {
+    WPF_CUDA(cudaEventRecord(h->cap_join, h->cap_side));
+    WPF_CUDA(cudaStreamWaitEvent(h->stream, h->cap_join, 0));
+    return WPF_OK;
+}
+
 // ---- step control kernels ------------------------------------------------------
 // The dt law of wPFAW3D.f90:2227-2230, dt = dt_c * min(dt_a, taumin), with
 // dt_c = tfac * dx^2 / (2 eps^2) and dt_a = eps^2 / D, taumin from the key the
@@ -138,6 +152,11 @@ int step_graph_prepare(wpf_handle* h) {
         WPF_CUDA(cudaMallocHost((void**)&h->gdsc_host, S_COUNT * sizeof(double)));
         h->gctl_dirty = true;
     }
+    if (!h->cap_side) {
+        WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_side, cudaStreamNonBlocking));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->cap_fork, cudaEventDisableTiming));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->cap_join, cudaEventDisableTiming));
+    }
     return WPF_OK;
 }
 
@@ -162,9 +181,8 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     h->kf_valid = kv;
     if (rc) return rc;
     n->fixed += h->nlaunch - l0;
-    if ((rc = solve_capture(h, b, n))) return rc;
+    if ((rc = solve_capture(h, b, n))) return rc;   // the solve and the fused update
     l0 = h->nlaunch;
-    if ((rc = phys_capture_update(h, &c->dt))) return rc;
     WPF_LAUNCH(h, KC_OTHER, k_step_end<<<1, 32, 0, s>>>(c));
     WPF_CUDA(cudaGetLastError());
     WPF_CUDA(cudaMemcpyAsync(h->gctl_host, c, sizeof(StepCtl), cudaMemcpyDeviceToHost, s));

@@ -249,6 +249,8 @@ struct wpf_handle {
     wpf::StepCtl* gctl_host;
     double* gdsc_host;
     bool gctl_dirty;         // the host-driven path ran since the last graph step
+    cudaStream_t cap_side;   // second branch of a captured step
+    cudaEvent_t cap_fork, cap_join;
     static constexpr int MAX_STEP_GRAPHS = 12;
     struct StepGraph {
         const void* key[6];
@@ -448,10 +450,14 @@ int ensure_per_routine_arrays(wpf_handle* h);
 int dev_alloc(wpf_handle* h, void** p, size_t bytes);
 
 // device-resident step (wpf_graph.cu, wpf_solver.cu, wpf_physics.cu)
-// capture the solve (Dirichlet values .. pressure halo) into b, in capture on entry and exit
+// capture the solve and the fused update (Dirichlet values .. new phase and
+// concentration) into b, in capture on entry and exit
 int solve_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
-// capture the fused update with dt read from *dtp (launches only, no host state change)
-int phys_capture_update(wpf_handle* h, const double* dtp);
+// capture the fused update on stream s with dt read from *dtp (launches only)
+int phys_capture_update(wpf_handle* h, const double* dtp, cudaStream_t s);
+// a second stream joins / leaves the capture running on h->stream
+int gb_fork(wpf_handle* h);
+int gb_join(wpf_handle* h);
 bool step_graph_ready(const wpf_handle* h, int itime);
 int step_graph_prepare(wpf_handle* h);           // allocations a capture needs
 int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);

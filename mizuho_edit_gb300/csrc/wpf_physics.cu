@@ -781,18 +781,16 @@ __global__ void k_step_slots_reset(double* dsc) {
     u[S_NWORK] = 0ull;
 }
 
-int phys_capture_update(wpf_handle* h, const double* dtp) {
+int phys_capture_update(wpf_handle* h, const double* dtp, cudaStream_t s) {
     const Grid& g = h->g;
     int* nwork = reinterpret_cast<int*>(h->dsc + S_NWORK);
-    WPF_LAUNCH(h, KC_OTHER, k_step_slots_reset<<<1, 32, 0, h->stream>>>(h->dsc));
-    WPF_CUDA(cudaEventRecordWithFlags(h->ev[2], h->stream, cudaEventRecordExternal));
-    WPF_LAUNCH(h, KC_FUSED, k_update_split<<<row_blocks(h, g), RB, 0, h->stream>>>(
+    WPF_LAUNCH(h, KC_OTHER, k_step_slots_reset<<<1, 32, 0, s>>>(h->dsc));
+    WPF_LAUNCH(h, KC_FUSED, k_update_split<<<row_blocks(h, g), RB, 0, s>>>(
         g, h->phase, h->concent, h->flags, h->phase_n, h->concent_n, h->work, nwork, h->phys.tau0,
         h->dsc));
-    WPF_LAUNCH(h, KC_FUSED, k_update_active<<<(unsigned)h->nsm * 2, RB, 0, h->stream>>>(
+    WPF_LAUNCH(h, KC_FUSED, k_update_active<<<(unsigned)h->nsm * 2, RB, 0, s>>>(
         g, h->dphys, h->phase, h->concent, h->pressure, h->T[0], h->T[1], h->T[2], h->flags,
         h->work, nwork, h->phase_n, h->concent_n, 0.0, h->dsc, dtp));
-    WPF_CUDA(cudaEventRecordWithFlags(h->ev[3], h->stream, cudaEventRecordExternal));
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
