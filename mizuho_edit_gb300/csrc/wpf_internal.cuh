@@ -192,7 +192,8 @@ struct wpf_handle {
     wpf_solver_opts opts;
     wpf::Hierarchy<double> h64;
     wpf::Hierarchy<float> h32;
-    double* r64;             // FP64 residual (mixed mode)
+    double* dsum;            // FP64 sum of a live cell's six face T (mixed mode: the
+                             // diagonal of the outer residual's diagonal-sum form)
     // extrapolated warm start (WPF_SOLVER_EXTRAPOLATE): the pressure increments
     // of the last two solves (ws[0] newest) and this solve's (ws[2]), FP32
     float* ws[3];

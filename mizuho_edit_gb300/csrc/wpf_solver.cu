@@ -54,7 +54,32 @@ constexpr int FX = SX + 4, FY = SY + 4;    // shared footprint: tile + 2-cell ri
 // FP64 outer residual.  r = qterm + sum_f T_f (p_nb - p_c) on free cells, 0 on
 // Dirichlet cells; accumulates ||r||^2 and, when want_b, ||b_ref||^2 with
 // b_ref the reference right-hand side (:803-825, :852-931).
+//
+// With D (the FP64 sum of the six face transmissibilities of each live cell)
+// the residual is formed as r = q + sum_f T_f p_nb - D p_c: seven FP64 FMAs
+// instead of six subtractions and six multiply-adds (the FP64 pipe bounds
+// these kernels on GB300).  The terms T p cancel where the differences T dp
+// did not, which raises the rounding floor of ||r||/||b|| by about the ratio
+// |p| / |dp| between neighbours (a few hundred on these grids): ~1e-14, far
+// below the 1e-8 of the mixed form, which alone uses it.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double resid_cell(double q, double p0, double pxp, double pxm, double pyp,
+                                             double pym, double pzp, double pzm, double txp, double txm,
+                                             double typ, double tym, double tzp, double tzm,
+                                             const double* __restrict__ D, long long n) {
+    if (D) {
+        double acc = fma(tzm, pzm, q);
+        acc = fma(tym, pym, acc);
+        acc = fma(txm, pxm, acc);
+        acc = fma(txp, pxp, acc);
+        acc = fma(typ, pyp, acc);
+        acc = fma(tzp, pzp, acc);
+        return fma(-D[n], p0, acc);
+    }
+    return q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
+                typ * (pyp - p0) + tzp * (pzp - p0));
+}
+
 template <typename R>
 __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict__ pr,
                                                 const double* __restrict__ Tx,
@@ -62,6 +87,7 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
                                                 const double* __restrict__ Tz,
                                                 const uint8_t* __restrict__ fl,
                                                 const double* __restrict__ qterm,
+                                                const double* __restrict__ D,
                                                 R* __restrict__ rout, double* dsc, int want_b,
                                                 const int* skip = nullptr,
                                                 float* __restrict__ zero_out = nullptr) {
@@ -85,8 +111,7 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
             const double tzp = Tz[n], tzm = Tz[n - sz];
             const double pxp = pr[n + 1], pxm = pr[n - 1], pyp = pr[n + sy], pym = pr[n - sy];
             const double pzp = pr[n + sz], pzm = pr[n - sz];
-            r = q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
-                     typ * (pyp - p0) + tzp * (pzp - p0));
+            r = resid_cell(q, p0, pxp, pxm, pyp, pym, pzp, pzm, txp, txm, typ, tym, tzp, tzm, D, n);
             if (want_b && (q != 0.0 || ((fl[n - sz] | fl[n - sy] | fl[n - 1] | fl[n + 1] |
                                          fl[n + sy] | fl[n + sz]) & F_DIR))) {
                 double bref = -q;
@@ -155,6 +180,10 @@ __device__ __forceinline__ R apply_l0(const R* __restrict__ cx, const R* __restr
 // r_ext = r0 - A'e_ext with A'e from the level-0 coefficients in precision R
 // (e is a small increment, so its rounding stays orders of magnitude below the
 // outer tolerance); writes rout = r_ext, dnew = e_ext, ||r_ext||^2 into S_RR64.
+// With D (the mixed form) r_ext is formed in R from r0 rounded to R: its
+// relative error, ~1e-7 |r0| / |r_ext|, only perturbs the right-hand side of
+// the first correction, and the pass that accepts the solve always takes a
+// plain FP64 residual.
 // With a learned correction e_net: also w = A'e_net, r_ext.w into S_RW and
 // w.w into S_WW, from which the host takes the step alpha = r.w / w.w that
 // minimises ||r_ext - alpha w|| (so the correction never raises the residual).
@@ -165,6 +194,7 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    const double* __restrict__ Tz,
                                                    const uint8_t* __restrict__ fl,
                                                    const double* __restrict__ qterm,
+                                                   const double* __restrict__ D,
                                                    const R* __restrict__ cx, const R* __restrict__ cy,
                                                    const R* __restrict__ cz,
                                                    const R* __restrict__ diag,
@@ -173,6 +203,7 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    R* __restrict__ rout, float* __restrict__ dnew,
                                                    double* dsc) {
     double rr1 = 0.0, rr0 = 0.0, bb = 0.0, rw = 0.0, ww = 0.0;
+    R rr1r = 0, rwr = 0, wwr = 0;   // the same sums in R (with D)
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
@@ -188,8 +219,7 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
             const double tzp = Tz[n], tzm = Tz[n - sz];
             const double pxp = pr[n + 1], pxm = pr[n - 1], pyp = pr[n + sy], pym = pr[n - sy];
             const double pzp = pr[n + sz], pzm = pr[n - sz];
-            r0 = q + (tzm * (pzm - p0) + tym * (pym - p0) + txm * (pxm - p0) + txp * (pxp - p0) +
-                      typ * (pyp - p0) + tzp * (pzp - p0));
+            r0 = resid_cell(q, p0, pxp, pxm, pyp, pym, pzp, pzm, txp, txm, typ, tym, tzp, tzm, D, n);
             // b_ref differs from -q only next to a Dirichlet cell: branch on
             // the neighbour flags so that interior cells issue no FP64 there
             const uint8_t dm = (fl[n - sz] | fl[n - sy] | fl[n - 1] | fl[n + 1] | fl[n + sy] |
@@ -205,18 +235,34 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                 bb += bref * bref;
             }
             e = e1[n];
-            r1 = r0 - (double)apply_l0(cx, cy, cz, diag, e1, n, sy, sz);
-            if (e2) {
-                const double w = (double)apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
-                rw += r1 * w;
-                ww += w * w;
+            if (D) {
+                const R r1r = (R)r0 - apply_l0(cx, cy, cz, diag, e1, n, sy, sz);
+                rout[n] = r1r;
+                rr1r += r1r * r1r;
+                if (e2) {
+                    const R w = apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+                    rwr += r1r * w;
+                    wwr += w * w;
+                }
+            } else {
+                r1 = r0 - (double)apply_l0(cx, cy, cz, diag, e1, n, sy, sz);
+                if (e2) {
+                    const double w = (double)apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+                    rw += r1 * w;
+                    ww += w * w;
+                }
             }
         }
-        rout[n] = (R)r1;
+        if (!D || (f & F_DIR)) {
+            rout[n] = (R)r1;
+            rr1 += r1 * r1;
+        }
         dnew[n] = e;
-        rr1 += r1 * r1;
         rr0 += r0 * r0;
     }
+    rr1 += (double)rr1r;
+    rw += (double)rwr;
+    ww += (double)wwr;
     block_add(rr1, dsc + S_RR64);
     block_add(rr0, dsc + S_RR0WS);
     block_add(bb, dsc + S_BB64);
@@ -268,19 +314,27 @@ __global__ void __launch_bounds__(RB) k_l0_coeffs(Grid g, const double* __restri
                                                   const uint8_t* __restrict__ fl,
                                                   R* __restrict__ cx, R* __restrict__ cy,
                                                   R* __restrict__ cz, R* __restrict__ diag,
-                                                  R* __restrict__ idiag) {
+                                                  R* __restrict__ idiag, double* __restrict__ dsum) {
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const bool live = !(fl[n] & F_DIR);
-        // each face converted once; the diagonal sums the six faces in R: FP64
-        // issue is scarce, and the FP32 operator only needs FP32 accuracy (the
-        // outer residual is FP64)
         const R tx = (R)Tx[n], ty = (R)Ty[n], tz = (R)Tz[n];
         cx[n] = (live && !(fl[n + 1] & F_DIR)) ? tx : (R)0;
         cy[n] = (live && !(fl[n + sy] & F_DIR)) ? ty : (R)0;
         cz[n] = (live && !(fl[n + sz] & F_DIR)) ? tz : (R)0;
-        const R d = tx + (R)Tx[n - 1] + ty + (R)Ty[n - sy] + tz + (R)Tz[n - sz];
+        R d;
+        if (dsum) {
+            // the FP64 diagonal of the outer residual's operator (its
+            // diagonal-sum form), from which the R diagonal is rounded
+            const double D = live ? Tx[n] + Tx[n - 1] + Ty[n] + Ty[n - sy] + Tz[n] + Tz[n - sz] : 0.0;
+            dsum[n] = D;
+            d = (R)D;
+        } else {
+            // each face converted once, the six summed in R: the R operator only
+            // needs R accuracy (the outer residual is FP64)
+            d = tx + (R)Tx[n - 1] + ty + (R)Ty[n - sy] + tz + (R)Tz[n - sz];
+        }
         const R dr = live ? d : (R)0;
         diag[n] = dr;
         idiag[n] = (live && dr > (R)0) ? (R)1 / dr : (R)0;
@@ -1070,12 +1124,15 @@ static void free_hierarchy(Hierarchy<R>& H) {
     H = Hierarchy<R>();
 }
 
+// The FP64 diagonal sums of the outer residual's diagonal-sum form (mixed form only).
+static double* resid_dsum(wpf_handle* h) { return h->opts.mode == WPF_SOLVER_MIXED ? h->dsum : nullptr; }
+
 template <typename R>
 static void build_level0(wpf_handle* h, Hierarchy<R>& H, cudaStream_t s) {
     const Grid& g = h->g;
     Level<R>& L0 = H.lv[0];
     WPF_LAUNCH(h, KC_COEF, k_l0_coeffs<R><<<row_blocks(h, g), RB, 0, s>>>(
-        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag));
+        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag, resid_dsum(h)));
 }
 
 template <typename R>
@@ -1444,7 +1501,7 @@ int solver_setup(wpf_handle* h) {
     if (h->opts.mode == WPF_SOLVER_MIXED) {
         rc = alloc_hierarchy(h, h->h32);
         if (rc) return rc;
-        if (!h->r64) return dev_alloc(h, (void**)&h->r64, sizeof(double) * h->g.total);
+        if (!h->dsum) return dev_alloc(h, (void**)&h->dsum, sizeof(double) * h->g.total);
         return WPF_OK;
     }
     return alloc_hierarchy(h, h->h64);
@@ -1459,8 +1516,8 @@ void solver_drop_graphs(wpf_handle* h) {
 int solver_free(wpf_handle* h) {
     free_hierarchy(h->h64);
     free_hierarchy(h->h32);
-    if (h->r64) cudaFree(h->r64);
-    h->r64 = nullptr;
+    if (h->dsum) cudaFree(h->dsum);
+    h->dsum = nullptr;
     for (int q = 0; q < 3; ++q) {
         if (h->ws[q]) cudaFree(h->ws[q]);
         h->ws[q] = nullptr;
@@ -1544,7 +1601,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             const bool net = h->ws_net && h->ws_hist >= 2;
             if (net && (rc = ws_net_correction(h))) return rc;
             WPF_LAUNCH(h, KC_RESID64, k_resid64_ws<R><<<rb, RB, 0, s>>>(
-                g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, H.lv[0].cx, H.lv[0].cy,
+                g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx, H.lv[0].cy,
                 H.lv[0].cz, H.lv[0].diag, h->ws_e[0], net ? h->ws_e[1] : nullptr, H.r, dnew, h->dsc));
             WPF_CUDA(cudaGetLastError());
             rc = read_slot(h, S_RR64, 5);
@@ -1579,7 +1636,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         if (plain) {
             if (pass == 0 && ws_on) WPF_CUDA(cudaMemsetAsync(dnew, 0, sizeof(float) * g.total, s));
             WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                              h->flags, h->qterm, H.r, h->dsc, pass == 0));
+                                                              h->flags, h->qterm, resid_dsum(h), H.r, h->dsc, pass == 0));
             WPF_CUDA(cudaGetLastError());
             rc = read_slot(h, S_RR64, 2);
             if (rc) return rc;
@@ -1795,15 +1852,15 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
         WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0], d,
                                                                    &c->wa));
         WPF_LAUNCH(h, KC_RESID64, k_resid64_ws<R><<<rb, RB, 0, s>>>(
-            g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, L0.cx, L0.cy, L0.cz, L0.diag,
+            g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
             h->ws_e[0], nullptr, H.r, dnew, d));
         WPF_LAUNCH(h, KC_OTHER, k_ctl_accept<<<1, 32, 0, s>>>(c, d));
         WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                                   h->flags, h->qterm, H.r, d, 1, &c->accept,
+                                                                   h->flags, h->qterm, resid_dsum(h), H.r, d, 1, &c->accept,
                                                                    dnew));
     } else {
         WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                                   h->flags, h->qterm, H.r, d, 1));
+                                                                   h->flags, h->qterm, resid_dsum(h), H.r, d, 1));
     }
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
                                                          mixed, h_pass));
@@ -1841,7 +1898,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
                                                                     ws_on ? h->ws_e[0] : nullptr, dnew, c));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_advance<<<1, 32, 0, s>>>(c, d));
     WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                               h->flags, h->qterm, H.r, d, 0));
+                                                               h->flags, h->qterm, resid_dsum(h), H.r, d, 0));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
                                                          mixed, h_pass));
     WPF_CUDA(cudaGetLastError());
