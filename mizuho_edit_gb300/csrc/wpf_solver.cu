@@ -154,17 +154,19 @@ __global__ void __launch_bounds__(RB) k_ws_build_ext(Grid g, const float* __rest
         a = ab[0];
         b = ab[1];
     }
-    double s2 = 0.0, q2 = 0.0;
+    // the two scales are sums of squares of FP32 data: FP32 per thread (a few
+    // hundred terms), FP64 across threads, no FP64 work per cell
+    float s2 = 0.f, q2 = 0.f;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const float v1 = d1[n], v2 = d2[n];
         e[n] = __fmaf_rn(a, v1, __fmul_rn(b, v2));
-        s2 += (double)v1 * v1;
-        const double dd = (double)v1 - (double)v2;
-        q2 += dd * dd;
+        s2 = __fmaf_rn(v1, v1, s2);
+        const float dd = v1 - v2;
+        q2 = __fmaf_rn(dd, dd, q2);
     }
-    block_add(s2, dsc + S_WSS2);
-    block_add(q2, dsc + S_WSD2);
+    block_add((double)s2, dsc + S_WSS2);
+    block_add((double)q2, dsc + S_WSD2);
 }
 
 template <typename R>
