@@ -56,6 +56,9 @@ def parse():
                          "fastest at 256^3 of 2, 3, 4 and a V-cycle (same PCG iterations as 2)")
     ap.add_argument("--breakdown", action="store_true",
                     help="time every kernel class (diagnostic run; adds event overhead)")
+    ap.add_argument("--plain-w-from", type=int, default=2,
+                    help="W-cycle level of the plain FP64 comparison run (2: its fewest PCG "
+                         "iterations; from level 3 it takes 7 instead of 5 at 256^3)")
     ap.add_argument("--nu", type=int, default=2, help="smoothing sweeps per side of a cycle")
     ap.add_argument("--sweep-min", type=int, default=0,
                     help="cells from which a level uses the pipelined sweep (0 = library default)")
@@ -83,7 +86,8 @@ def solver_kwargs(args, solver=None):
     """Solver options of the timed arm; solver="fp64" gives the plain method
     (FP64 MG-PCG started from the previous pressure, as the reference)."""
     plain = solver == "fp64"
-    return dict(solver=solver or args.solver, rtol=args.rtol, w_from_level=args.w_from,
+    return dict(solver=solver or args.solver, rtol=args.rtol,
+                w_from_level=args.plain_w_from if plain else args.w_from,
                 smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min,
                 graphs=not args.no_graphs, tma=not args.no_tma,
                 step_graph=not args.no_step_graph,
@@ -183,7 +187,8 @@ def config_of(args, world):
             "warm_start": ("time-extrapolated pressure with fallback to the previous pressure"
                            if args.warm_start == "extrap" and args.solver == "mixed"
                            else "previous pressure"),
-            "compared_with": "plain FP64 MG-PCG from the previous pressure (plain_fp64)",
+            "compared_with": f"plain FP64 MG-PCG from the previous pressure (plain_fp64; W-cycle "
+                             f"from level {args.plain_w_from})",
             "timed_steps": f"{args.spinup + args.warmup + 1}..{args.spinup + args.warmup + args.steps}"
                            f" of the run (spin-up {args.spinup} + warm-up {args.warmup} untimed)",
             "multigrid": {"w_cycle_from_level": args.w_from, "sweeps_per_side": args.nu,
