@@ -249,6 +249,7 @@ int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o) {
     h->opts = *o;
     h->ws_hist = 0;          // a new solver starts a new increment history
     h->ws_h1 = h->ws_h2 = 0.0;
+    h->rkeep_ok = false;
     if (!(h->opts.inner_rtol > 0 && h->opts.inner_rtol < 1)) h->opts.inner_rtol = 1e-4;
     if (h->opts.smooth_sweeps == 0) h->opts.smooth_sweeps = 2;
     return WPF_OK;
@@ -318,6 +319,7 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
     WPF_CUDA(cudaStreamSynchronize(h->stream));   // host vectors go out of scope
     h->have_wells = true;
     h->ws_hist = 0;   // new boundary conditions: the increment history no longer applies
+    h->rkeep_ok = false;
     step_graphs_drop(h);   // the step graphs bake in the well arrays
     return phys_set_dirichlet(h);
 }
@@ -399,6 +401,7 @@ int wpf_upload(wpf_handle* h, const double* krock, const double* phase, const do
         if ((rc = phys_set_dirichlet(h))) return rc;
     }
     h->vel_valid = false;
+    h->rkeep_ok = false;   // the kept residual no longer matches p and T
     if (krock) h->ws_klog_ready = false;   // the learned start's input statistics change
     if (phase || krock) {
         h->kf_valid = false;
@@ -644,3 +647,59 @@ int wpf_reduce(wpf_handle* h, wpf_diag* d) {
 }
 
 }  // extern "C"
+
+namespace wpf {
+// The integer-pipe conversions against the hardware ones: x -> FP32 must equal
+// __double2float_rn(x) wherever that is a normal number, zero, Inf or NaN (an
+// FP32-subnormal result flushes to a zero of the same sign), and FP32 -> FP64
+// must be exact for every FP32 value that is not subnormal.
+__global__ void k_check_conversions(const double* x, long long n, unsigned long long* bad) {
+    unsigned long long nb = 0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const double v = x[q];
+        const float ref = __double2float_rn(v);
+        const float got = f64_to_f32(v);
+        const unsigned ur = __float_as_uint(ref), ug = __float_as_uint(got);
+        const unsigned ar = ur & 0x7fffffffu;
+        bool ok;
+        if (ar > 0x7f800000u) ok = (ug & 0x7fffffffu) > 0x7f800000u;                 // NaN
+        else if (ar != 0u && ar < 0x00800000u) ok = ug == (ur & 0x80000000u);        // FP32 subnormal: flushed
+        else ok = ug == ur;
+        if (!ok) ++nb;
+        const float f = ref;
+        const unsigned af = __float_as_uint(f) & 0x7fffffffu;
+        if (!(af != 0u && af < 0x00800000u) && af <= 0x7f800000u) {
+            const double back = f32_to_f64(f);
+            if (__double_as_longlong(back) != __double_as_longlong((double)f)) ++nb;
+        }
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+}  // namespace wpf
+
+extern "C" int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatches) {
+    using namespace wpf;
+    if (!host_values || n < 0 || !mismatches) return WPF_ERR_ARG;
+    *mismatches = 0;
+    if (n == 0) return WPF_OK;
+    double* d = nullptr;
+    unsigned long long* bad = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * n) != cudaSuccess || cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess) {
+        cudaGetLastError();
+        if (d) cudaFree(d);
+        return WPF_ERR_NOMEM;
+    }
+    unsigned long long nb = 0;
+    int rc = WPF_OK;
+    if (cudaMemcpy(d, host_values, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(bad, 0, sizeof(*bad)) != cudaSuccess)
+        rc = WPF_ERR_CUDA;
+    if (!rc) {
+        k_check_conversions<<<256, 256>>>(d, n, bad);
+        if (cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost) != cudaSuccess) rc = WPF_ERR_CUDA;
+    }
+    cudaFree(d);
+    cudaFree(bad);
+    *mismatches = (int64_t)nb;
+    return rc;
+}

@@ -24,7 +24,7 @@ namespace {
 
 struct EnsGraph {
     std::vector<unsigned long long> uid, epoch;
-    std::vector<const void*> keys;   // six buffer pointers per member
+    std::vector<const void*> keys;   // STEP_KEY entries per member
     std::vector<StepCounts> n;
     cudaGraphExec_t exec = nullptr;
     unsigned long long last_use = 0;
@@ -49,11 +49,11 @@ int ensemble_graph_step(const std::vector<wpf_handle*>& mem, const std::vector<i
         if (rc) return rc;
     }
     std::vector<unsigned long long> uid(n), epoch(n);
-    std::vector<const void*> keys(6 * (size_t)n);
+    std::vector<const void*> keys((size_t)STEP_KEY * n);
     for (int m = 0; m < n; ++m) {
         uid[m] = mem[m]->uid;
         epoch[m] = mem[m]->epoch;
-        step_graph_key(mem[m], &keys[6 * (size_t)m]);
+        step_graph_key(mem[m], &keys[(size_t)STEP_KEY * m]);
     }
     std::lock_guard<std::mutex> lk(ens_mu);
     EnsGraph* e = nullptr;

@@ -174,14 +174,19 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     if ((rc = gb_begin(b))) return rc;
     long long l0 = h->nlaunch;
     WPF_LAUNCH(h, KC_OTHER, k_step_begin<<<1, 32, 0, s>>>(c, h->dsc, dt_c, dt_a));
-    const bool tc = h->t_current, tp = h->t_from_prev, kv = h->kf_valid;
+    const bool tc = h->t_current, tp = h->t_from_prev, kv = h->kf_valid, rko = h->rkeep_ok;
     rc = phys_permeability(h, false);
     h->t_current = tc;
     h->t_from_prev = tp;
     h->kf_valid = kv;
-    if (rc) return rc;
+    if (rc) {
+        h->rkeep_ok = rko;
+        return rc;
+    }
     n->fixed += h->nlaunch - l0;
-    if ((rc = solve_capture(h, b, n))) return rc;   // the solve and the fused update
+    rc = solve_capture(h, b, n);   // the solve and the fused update (reads rkeep_ok as set above)
+    h->rkeep_ok = rko;
+    if (rc) return rc;
     l0 = h->nlaunch;
     WPF_LAUNCH(h, KC_OTHER, k_step_end<<<1, 32, 0, s>>>(c));
     WPF_CUDA(cudaGetLastError());
@@ -239,6 +244,8 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     h->kf_valid = false;
     h->t_from_prev = true;   // T came from the phase now in phase_n
     h->t_current = false;
+    // every graph step ends on a plain residual pass of the final pressure
+    h->rkeep_ok = h->rkeep && h->opts.mode == WPF_SOLVER_MIXED && c.status != WPF_ERR_NONFINITE;
     const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter;
     h->nlaunch += launches;
     int rc = c.status;
@@ -281,6 +288,8 @@ void step_graph_key(const wpf_handle* h, const void** k) {
     // calcPermeability recomputes only the faces whose cells changed phase when
     // T came from the phase now in phase_n (the last step), else every face
     k[5] = h->t_from_prev ? h->phase_n : nullptr;
+    // and then corrects the kept FP64 residual, which pass 0 reads
+    k[6] = (h->t_from_prev && h->rkeep && h->rkeep_ok) ? h->rkeep : nullptr;
 }
 
 // Upload the increment step sizes when the host-driven path changed them.
@@ -296,7 +305,7 @@ int step_graph_sync_ctl(wpf_handle* h) {
 int step_graph_run(wpf_handle* h, wpf_step_stats* st, double* dt_out) {
     int rc = step_graph_prepare(h);
     if (rc) return rc;
-    const void* key[6];
+    const void* key[STEP_KEY];
     step_graph_key(h, key);
     int slot = -1;
     for (int q = 0; q < h->nsg; ++q)

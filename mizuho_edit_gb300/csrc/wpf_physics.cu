@@ -242,33 +242,66 @@ __device__ __forceinline__ void flush_step_reductions(double tau, int over, doub
 // prev != null: skip a face-cell whose four cells have bitwise the same phase
 // as in prev, the field T was last computed from (T is then unchanged).
 // ---------------------------------------------------------------------------
+// With rk (the FP64 outer residual of the current pressure under the old T):
+// every recomputed face f between cells a and b whose T changed adds
+// (T_new - T_old)(p_b - p_a) to the residual of a live cell a (and the mirror
+// term to b), so that rk becomes the residual under the new T without a pass
+// over the grid (the update changes the phase of a few per cent of the cells).
+// Returns the owner cell a's share (summed by the caller into one atomic) and
+// adds the neighbour's share to rk[b].
+__device__ __forceinline__ double resid_face_delta(double* rk, const uint8_t* __restrict__ fl,
+                                                   const double* __restrict__ pr, long long a, long long b,
+                                                   double p_a, double dT) {
+    if (dT == 0.0) return 0.0;
+    const double d = dT * (pr[b] - p_a);
+    if (!(fl[b] & F_DIR)) atomicAdd(rk + b, -d);
+    return d;
+}
+
 __global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
                                const double* __restrict__ prev, const double* __restrict__ kr,
                                double* __restrict__ Tx, double* __restrict__ Ty,
                                double* __restrict__ Tz, double* __restrict__ Kx,
-                               double* __restrict__ Ky, double* __restrict__ Kz, double inv_mu) {
+                               double* __restrict__ Ky, double* __restrict__ Kz, double inv_mu,
+                               double* rk = nullptr, const uint8_t* __restrict__ fl = nullptr,
+                               const double* __restrict__ pr = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
     if (i > g.nx || j > g.ny || k > g.nz) return;
     const long long n = g.at(i, j, k);
-    if (prev && bits(ph[n]) == bits(prev[n]) && bits(ph[n + 1]) == bits(prev[n + 1]) &&
-        bits(ph[n + g.P]) == bits(prev[n + g.P]) && bits(ph[n + g.S]) == bits(prev[n + g.S]))
-        return;
+    // with prev: a face is recomputed only when one of its two cells changed
+    // phase (the harmonic means are FP64 divisions, the costliest work here)
+    bool fx = true, fy = true, fz = true;
+    if (prev) {
+        const bool c0 = bits(ph[n]) != bits(prev[n]);
+        fx = c0 || bits(ph[n + 1]) != bits(prev[n + 1]);
+        fy = c0 || bits(ph[n + g.P]) != bits(prev[n + g.P]);
+        fz = c0 || bits(ph[n + g.S]) != bits(prev[n + g.S]);
+        if (!(fx || fy || fz)) return;
+    }
     auto K0 = [&](long long m) {
         const double f = 0.5 * (1.0 + ph[m]);
         return P.kwh * f + kr[m] * (1.0 - f);
     };
     const double a = K0(n);
-    const double bx = K0(n + 1), by = K0(n + g.P), bz = K0(n + g.S);
-    const double kx = 2.0 * a * bx / (a + bx);
-    const double ky = 2.0 * a * by / (a + by);
-    const double kz = 2.0 * a * bz / (a + bz);
     const bool in_j = j >= 1 && j <= g.ny, in_k = k >= 1 && k <= g.nz, in_i = i >= 1 && i <= g.nx;
-    Tx[n] = (i >= 1 && i < g.nx && in_j && in_k) ? kx * inv_mu : 0.0;
-    Ty[n] = (j >= 1 && j < g.ny && in_i && in_k) ? ky * inv_mu : 0.0;
-    Tz[n] = (k >= 1 && k < g.nz && in_i && in_j) ? kz * inv_mu : 0.0;
-    if (Kx) { Kx[n] = kx; Ky[n] = ky; Kz[n] = kz; }
+    const double p_a = rk ? pr[n] : 0.0;
+    double own = 0.0;
+    // face towards m (owner n): T = 2 a b / (a + b) / mu, 0 outside `inside`
+    auto face = [&](long long m, bool inside, double* __restrict__ T, double* __restrict__ Kf) {
+        const double b = K0(m);
+        const double kf = 2.0 * a * b / (a + b);
+        const double t = inside ? kf * inv_mu : 0.0;
+        if (rk) own += resid_face_delta(rk, fl, pr, n, m, p_a, t - T[n]);
+        T[n] = t;
+        if (Kf) Kf[n] = kf;
+    };
+    if (fx) face(n + 1, i >= 1 && i < g.nx && in_j && in_k, Tx, Kx);
+    if (fy) face(n + g.P, j >= 1 && j < g.ny && in_i && in_k, Ty, Ky);
+    if (fz) face(n + g.S, k >= 1 && k < g.nz && in_i && in_j, Tz, Kz);
+    // boundary faces stay 0 (dT = 0): only interior pairs change the residual
+    if (rk && own != 0.0 && !(fl[n] & F_DIR)) atomicAdd(rk + n, own);
 }
 
 // K0 over every cell of the halo grid (:567-574), for downloads only.
@@ -662,10 +695,13 @@ int phys_permeability(wpf_handle* h, bool materialise) {
     // T is still valid for every face whose two cells kept their phase since
     // the fused update that produced the current phase (t_from_prev).
     const double* prev = (!materialise && h->t_from_prev) ? h->phase_n : nullptr;
+    // the kept outer residual follows T only through the incremental form
+    const bool keep = prev && h->rkeep && h->rkeep_ok;
+    h->rkeep_ok = keep;
     WPF_LAUNCH(h, KC_PERM, k_permeability<<<gr, b, 0, h->stream>>>(
         g, h->phys, h->phase, prev, h->krock, h->T[0], h->T[1], h->T[2],
         materialise ? h->Kf[0] : nullptr, materialise ? h->Kf[1] : nullptr,
-        materialise ? h->Kf[2] : nullptr, inv_mu(h)));
+        materialise ? h->Kf[2] : nullptr, inv_mu(h), keep ? h->rkeep : nullptr, h->flags, h->pressure));
     WPF_CUDA(cudaGetLastError());
     h->kf_valid = materialise;
     h->t_current = true;

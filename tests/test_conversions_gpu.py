@@ -1,0 +1,42 @@
+"""The FP64 <-> FP32 conversions the kernels perform on the integer pipe
+agree with the hardware conversions: round to nearest even into FP32 over
+the whole FP32 normal range (ties, carries into the exponent, the overflow
+boundary), Inf and NaN, and exact FP32 -> FP64; FP32-subnormal results flush
+to zero by design."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _values():
+    rng = np.random.default_rng(7)
+    parts = [
+        rng.standard_normal(200000) * 10.0 ** rng.integers(-45, 45, 200000),
+        rng.uniform(-1, 1, 100000),
+        np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 3.4028234663852886e38,
+                  3.4028235677973366e38, 3.40282357e38, 1e39, -1e39, 1.1754943508222875e-38,
+                  1.1754942e-38, 1e-40, -1e-45, 5e-324, np.finfo(np.float64).max]),
+    ]
+    # exact ties and near-ties at the 29 dropped mantissa bits
+    base = rng.uniform(1, 2, 50000).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(base.astype(np.float32)).astype(np.float64)
+    parts += [base + ulp / 2, base - ulp / 2, base + ulp / 2 * (1 + 2.0 ** -40), (base + ulp / 2) * 2.0 ** 100,
+              -(base + ulp / 2) * 2.0 ** -100]
+    # every FP32 exponent, mantissa all ones (rounding carries into the exponent)
+    e = np.arange(-126, 128, dtype=np.float64)
+    parts.append((2.0 - 2.0 ** -24) * 2.0 ** e)
+    parts.append((2.0 - 2.0 ** -23) * 2.0 ** e)
+    return np.ascontiguousarray(np.concatenate(parts), dtype=np.float64)
+
+
+def test_integer_pipe_conversions_match_hardware():
+    from mizuho_edit_gb300 import capi
+    L = capi.load()
+    v = _values()
+    bad = C.c_int64(-1)
+    capi.check(L.wpf_check_conversions(v.ctypes.data_as(capi.DP), v.size, C.byref(bad)),
+               "wpf_check_conversions")
+    assert bad.value == 0
