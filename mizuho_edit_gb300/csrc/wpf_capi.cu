@@ -132,6 +132,8 @@ static void free_all(wpf_handle* h) {
         if (p) cudaFree(p);
     if (h->flags) cudaFree(h->flags);
     if (h->work) cudaFree(h->work);
+    for (int q = 0; q < 2; ++q)
+        if (h->bact[q]) cudaFree(h->bact[q]);
     if (h->snap) cudaFree(h->snap);
     if (h->snap_ready) cudaEventDestroy(h->snap_ready);
     if (h->snap_done) cudaEventDestroy(h->snap_done);
@@ -320,6 +322,7 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
     h->have_wells = true;
     h->ws_hist = 0;   // new boundary conditions: the increment history no longer applies
     h->rkeep_ok = false;
+    h->bact_ok = false;   // the well flags enter the update's classification
     step_graphs_drop(h);   // the step graphs bake in the well arrays
     return phys_set_dirichlet(h);
 }
@@ -402,6 +405,7 @@ int wpf_upload(wpf_handle* h, const double* krock, const double* phase, const do
     }
     h->vel_valid = false;
     h->rkeep_ok = false;   // the kept residual no longer matches p and T
+    if (phase || concent) h->bact_ok = false;   // the update's brick activity no longer holds
     if (krock) h->ws_klog_ready = false;   // the learned start's input statistics change
     if (phase || krock) {
         h->kf_valid = false;

@@ -142,7 +142,7 @@ int step_graph_prepare(wpf_handle* h) {
     int rc = solver_setup(h);
     if (rc) return rc;
     const Grid& g = h->g;
-    if (!h->work && (rc = dev_alloc(h, (void**)&h->work, sizeof(int) * (size_t)g.nx * g.ny * g.nz))) return rc;
+    if ((rc = update_alloc(h))) return rc;
     if (ws_enabled(h) && !h->ws_e[0] && (rc = dev_alloc(h, (void**)&h->ws_e[0], sizeof(float) * g.total)))
         return rc;
     if (!h->gctl) {
@@ -240,6 +240,7 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     }
     double* t = h->phase; h->phase = h->phase_n; h->phase_n = t;
     t = h->concent; h->concent = h->concent_n; h->concent_n = t;
+    update_advance_bricks(h);
     h->vel_valid = false;
     h->kf_valid = false;
     h->t_from_prev = true;   // T came from the phase now in phase_n
@@ -290,6 +291,8 @@ void step_graph_key(const wpf_handle* h, const void** k) {
     k[5] = h->t_from_prev ? h->phase_n : nullptr;
     // and then corrects the kept FP64 residual, which pass 0 reads
     k[6] = (h->t_from_prev && h->rkeep && h->rkeep_ok) ? h->rkeep : nullptr;
+    // the update skips the bricks that were quiescent in the last update
+    k[7] = h->bact_ok ? h->bact[0] : nullptr;
 }
 
 // Upload the increment step sizes when the host-driven path changed them.
