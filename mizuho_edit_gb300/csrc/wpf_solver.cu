@@ -648,6 +648,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             }
         }
     };
+    const bool corrects = !ZERO && xc != nullptr;   // this sweep adds the coarse correction
     // Updated value of the cell at slot column w, slot row c (R1 row) of plane
     // k; neighbours = false when they are all known to be zero (first colour
     // of the zero-guess sweep).
@@ -672,9 +673,12 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     const bool fj_ok = f_on && fj >= 1 && fj <= g.ny;
     // Second colour of a plane on the tile: thread t < 16*SY takes the m-th
     // cell of that colour in tile row r; the values stay in shared memory.
+    // (the last PS*SY threads: with the pipelined order of the TMA path the two
+    // colours share a phase, and 42 threads then take one cell of each)
     constexpr int PS = SX / 2;
-    const bool s_on = tid < PS * SY;
-    const int sr = s_on ? tid / PS : 0, sm2 = tid - sr * PS;
+    const int stid = tid - (NT - PS * SY);
+    const bool s_on = stid >= 0;
+    const int sr = s_on ? stid / PS : 0, sm2 = stid - sr * PS;
     const int sj = j0 + sr;
     const int spar = (c0 + 1 - i0 - sj) & 1;
     const bool sj_ok = s_on && sj <= g.ny;
@@ -715,23 +719,57 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     __syncthreads();
     first_colour(k0, slot(k0), slot(k0 - 1), slot(k0 + 1));
     int sk = slot_index(k0);                  // slot of plane k, advanced by one per plane
-    for (int k = k0; k <= k1; ++k) {
-        const int skm1 = sk == 0 ? NSLOT - 1 : sk - 1;
-        const int skp1 = sk == NSLOT - 1 ? 0 : sk + 1;
-        const int skp2 = skp1 == NSLOT - 1 ? 0 : skp1 + 1;
-        if (TMA) fence_proxy_async();         // this thread's generic accesses before the next copies
-        issue(k + 4);                         // the slot of plane k-3, idle since k-2
-        if (TMA) landed(k + 2);
-        else cp_async_wait<2>();              // plane k+2 landed
-        correct(k + 2);
+    if (TMA) {
+        // One phase and one block barrier per plane: the first colour of plane
+        // k+1 and the second colour of plane k-1 share a phase.  The first
+        // colour reads only old second-colour values (planes k..k+2), which
+        // the second colour of plane k-1 does not write; the second colour of
+        // k-1 reads the first colours of planes k-2..k, finished before the
+        // last barrier.  Live planes k-2..k+2 plus two in flight fill the
+        // seven slots; the copies of plane k+4 go to the slot of plane k-3,
+        // whose last readers (second colour of k-2, write-out of k-3) and
+        // fenced writers finished before the last barrier.  Every thread
+        // waits on the plane's mbarrier itself, which makes the landed copies
+        // visible to it; only the coarse correction, written by each thread
+        // into its own chunks of plane k+2 and read by the others, takes a
+        // barrier more.
+        for (int k = k0; k <= k1 + 1; ++k) {
+            const int skm1 = sk == 0 ? NSLOT - 1 : sk - 1;
+            const int skm2 = skm1 == 0 ? NSLOT - 1 : skm1 - 1;
+            const int skp1 = sk == NSLOT - 1 ? 0 : sk + 1;
+            const int skp2 = skp1 == NSLOT - 1 ? 0 : skp1 + 1;
+            fence_proxy_async();              // this thread's generic accesses before the next copies
+            if (k <= k1) {
+                issue(k + 4);
+                landed(k + 2);
+                if (corrects) {
+                    correct(k + 2);
+                    __syncthreads();
+                }
+            }
+            if (k - 2 >= k0) write_out(k - 2, slots[skm2]);
+            if (k <= k1) first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
+            if (k - 1 >= k0) second_colour(k - 1, slots[skm1], slots[skm2], slots[sk]);
+            __syncthreads();
+            sk = skp1;
+        }
+    } else {
+        for (int k = k0; k <= k1; ++k) {
+            const int skm1 = sk == 0 ? NSLOT - 1 : sk - 1;
+            const int skp1 = sk == NSLOT - 1 ? 0 : sk + 1;
+            const int skp2 = skp1 == NSLOT - 1 ? 0 : skp1 + 1;
+            issue(k + 4);                     // the slot of plane k-3, idle since k-2
+            cp_async_wait<2>();               // plane k+2 landed
+            correct(k + 2);
+            __syncthreads();
+            if (k > k0) write_out(k - 1, slots[skm1]);
+            first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
+            __syncthreads();
+            second_colour(k, slots[sk], slots[skm1], slots[skp1]);
+            sk = skp1;
+        }
         __syncthreads();
-        if (k > k0) write_out(k - 1, slots[skm1]);
-        first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
-        __syncthreads();
-        second_colour(k, slots[sk], slots[skm1], slots[skp1]);
-        sk = skp1;
     }
-    __syncthreads();
     write_out(k1, slot(k1));
     if (TMA) {   // the copies still in flight land before the block exits
         landed(k1 + 3);
