@@ -191,6 +191,11 @@ int wpf_create(const wpf_params* p, wpf_handle** out) {
     h->nsm = 1;
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
     if (h->nsm < 1) h->nsm = 1;
+    int pma = 0, pmh = 0;
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, h->device);
+    cudaDeviceGetAttribute(&pmh, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device);
+    h->host_pageable_direct = pma == 1 && pmh == 1;
+    cudaGetLastError();
     int rc = WPF_OK;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) rc = WPF_ERR_CUDA;
     for (int e = 0; e < 4 && !rc; ++e)
@@ -332,6 +337,23 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
 // copy through a dense staging buffer and is re-pitched on the device (block
 // = one row of nx+2 values): row-by-row 2D copies of 2 KB rows run far below
 // the link's bandwidth.
+// Host layout -> pitched device field, writing only the values that differ
+// bitwise from the device copy and flagging *changed if any did.
+__global__ void k_repitch_in(Grid g, const double* __restrict__ src, double* __restrict__ dst, int* changed) {
+    const int w = g.nx + 2;
+    const long long row = blockIdx.x;
+    const long long dense = row * w, pitched = g.at(0, 0, 0) + row * g.P;
+    int chg = 0;
+    for (int i = threadIdx.x; i < w; i += blockDim.x) {
+        const double v = src[dense + i];
+        if (__double_as_longlong(dst[pitched + i]) != __double_as_longlong(v)) {
+            dst[pitched + i] = v;
+            chg = 1;
+        }
+    }
+    if (__syncthreads_or(chg) && threadIdx.x == 0) *changed = 1;
+}
+
 __global__ void k_repitch(Grid g, const double* __restrict__ src, double* __restrict__ dst,
                           int to_pitched) {
     const int w = g.nx + 2;
@@ -368,20 +390,47 @@ static int ensure_staging(wpf_handle* h) {
     return dev_alloc(h, (void**)&h->staging, sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2));
 }
 
-static int copy_field_in(wpf_handle* h, double* dst, const double* src) {
+// The address through which a kernel reads or writes the host array p in
+// place, or null when it has to go through a staging copy: page-locked
+// memory (its mapped device address) always; ordinary pageable memory when
+// the device reaches it through the host's page tables (GB300 with its Grace
+// host over the coherent NVLink-C2C), which the handle queried at creation.
+static const void* host_direct(const wpf_handle* h, const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered && h->host_pageable_direct) return p;
+    return nullptr;
+}
+
+// changed: device int set when any value differs from the device copy
+static int copy_field_in(wpf_handle* h, double* dst, const double* src, int* changed) {
     const Grid& g = h->g;
-    int rc = ensure_staging(h);
-    if (rc) return rc;
-    const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
-    WPF_CUDA(cudaMemcpyAsync(h->staging, src, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
-        g, h->staging, dst, 1));
+    const double* from = static_cast<const double*>(host_direct(h, src));   // read in place
+    if (!from) {
+        int rc = ensure_staging(h);
+        if (rc) return rc;
+        const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+        WPF_CUDA(cudaMemcpyAsync(h->staging, src, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        from = h->staging;
+    }
+    WPF_LAUNCH(h, KC_OTHER, k_repitch_in<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+        g, from, dst, changed));
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
 
 static int copy_field_out(wpf_handle* h, double* dst, const double* src) {
     const Grid& g = h->g;
+    if (double* hd = static_cast<double*>(const_cast<void*>(host_direct(h, dst)))) {   // write in place
+        WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+            g, src, hd, 0));
+        WPF_CUDA(cudaGetLastError());
+        return WPF_OK;
+    }
     int rc = ensure_staging(h);
     if (rc) return rc;
     const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
@@ -396,23 +445,36 @@ int wpf_upload(wpf_handle* h, const double* krock, const double* phase, const do
                const double* pressure) {
     if (!h) return WPF_ERR_ARG;
     int rc;
-    if (krock) { if ((rc = copy_field_in(h, h->krock, krock))) return rc; if ((rc = phys_halo(h, h->krock))) return rc; }
-    if (phase) { if ((rc = copy_field_in(h, h->phase, phase))) return rc; if ((rc = phys_halo(h, h->phase))) return rc; }
-    if (concent) { if ((rc = copy_field_in(h, h->concent, concent))) return rc; if ((rc = phys_halo(h, h->concent))) return rc; }
+    // each field is compared bitwise with the device copy as it is written:
+    // only a field that changed invalidates the state derived from it (a
+    // host driver that sends back what it downloaded keeps the incremental
+    // permeability, the kept residual and the quiescent bricks)
+    int* chg = reinterpret_cast<int*>(h->dsc + S_UPL0);   // krock, phase, concent, pressure
+    WPF_CUDA(cudaMemsetAsync(chg, 0, 4 * sizeof(int), h->stream));
+    if (krock) { if ((rc = copy_field_in(h, h->krock, krock, chg + 0))) return rc; if ((rc = phys_halo(h, h->krock))) return rc; }
+    if (phase) { if ((rc = copy_field_in(h, h->phase, phase, chg + 1))) return rc; if ((rc = phys_halo(h, h->phase))) return rc; }
+    if (concent) { if ((rc = copy_field_in(h, h->concent, concent, chg + 2))) return rc; if ((rc = phys_halo(h, h->concent))) return rc; }
     if (pressure) {
-        if ((rc = copy_field_in(h, h->pressure, pressure))) return rc;
+        if ((rc = copy_field_in(h, h->pressure, pressure, chg + 3))) return rc;
         if ((rc = phys_set_dirichlet(h))) return rc;
     }
-    h->vel_valid = false;
-    h->rkeep_ok = false;   // the kept residual no longer matches p and T
-    if (phase || concent) h->bact_ok = false;   // the update's brick activity no longer holds
-    if (krock) h->ws_klog_ready = false;   // the learned start's input statistics change
-    if (phase || krock) {
+    WPF_CUDA(cudaMemcpyAsync(h->hsc + S_UPL0, h->dsc + S_UPL0, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    int c[4];
+    memcpy(c, h->hsc + S_UPL0, sizeof(c));
+    const bool ck = krock && c[0], cp = phase && c[1], cc = concent && c[2], cpr = pressure && c[3];
+    if (ck || cp || cpr) {
+        h->vel_valid = false;
+        h->rkeep_ok = false;   // the kept residual no longer matches p and T
+    }
+    if (cp || cc) h->bact_ok = false;   // the update's brick activity no longer holds
+    if (ck) h->ws_klog_ready = false;   // the learned start's input statistics change
+    if (cp || ck) {
         h->kf_valid = false;
         h->t_current = false;
         h->t_from_prev = false;
     }
-    WPF_CUDA(cudaStreamSynchronize(h->stream));
     return WPF_OK;
 }
 

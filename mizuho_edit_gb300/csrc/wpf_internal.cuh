@@ -66,6 +66,7 @@ enum Slot {
     S_DPH2,             // sum of the squared phase change of the last step (its scale)
     S_KLOG0, S_KLOG1,   // sum of log K_rock and of its square (input normalisation)
     S_KERR,             // set (int) by a kernel whose bounded wait ran out
+    S_UPL0, S_UPL1,     // wpf_upload: one int per field whose values changed (4 ints)
     S_COUNT = 32
 };
 
@@ -211,6 +212,7 @@ struct wpf_handle {
     double ws_hn, ws_h1, ws_h2;   // step sizes: this step, previous, one before (0 = unknown)
     long long ws_fallbacks;  // solves whose extrapolated start was rejected
     double* staging;         // dense halo-array staging for host copies (lazily allocated)
+    bool host_pageable_direct;   // kernels reach pageable host memory in place (host page tables)
     struct wpf_net* ws_net;  // learned warm start (not owned), or null
     float* ws_e[2];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output)
     uint16_t* ws_in;         // net input (bf16, net grid, 16 channels)

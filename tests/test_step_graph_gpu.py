@@ -52,6 +52,21 @@ def _sim(case, **kw):
     return Simulation(case.params, case.permeab_rock, case.phase, case.concent, **kw)
 
 
+def _replace(sim, name):
+    """Upload different values of a field and then its own values again: the
+    two uploads change the field, so the state derived from it is dropped
+    (an upload of unchanged values keeps it)."""
+    import numpy as np
+    f = sim.download(name)
+    args = {"phase": [None, None, None, None], "concent": [None, None, None, None],
+            "pressure": [None, None, None, None]}[name]
+    slot = {"phase": 1, "concent": 2, "pressure": 3}[name]
+    for v in (np.zeros_like(f), f):
+        a = list(args)
+        a[slot] = v
+        sim.upload(*a)
+
+
 def _run(case, nsteps, allow_unconverged=False, between=None, **kw):
     with _sim(case, **kw) as sim:
         stats = []
@@ -88,9 +103,11 @@ def test_step_graph_pipelined_levels():
 
 
 def test_step_graph_after_upload_matches():
-    """A host round trip of the fields between steps: wpf_upload of the phase
-    rules out the incremental permeability update, so the next step takes the
-    graph captured with every face recomputed, as the host-driven step does."""
+    """Host round trips of the fields between steps: an upload of the values
+    the device holds keeps the derived state (steps 4, 5), a changed phase
+    rules out the incremental permeability update (step 8), so that step
+    takes the graph captured with every face recomputed, as the host-driven
+    step does."""
     case = _case(seed=11)
     kw = dict(solver="mixed", rtol=1e-8, extrapolate=True)
 
@@ -98,7 +115,7 @@ def test_step_graph_after_upload_matches():
         f = sim.download(*FIELDS)
         sim.upload(None, f["phase"], f["concent"], f["pressure"])
 
-    between = {s: roundtrip for s in (4, 5, 8)}
+    between = {4: roundtrip, 5: roundtrip, 8: lambda sim: _replace(sim, "phase")}
     _assert_same(_run(case, 10, between=between, **kw),
                  _run(case, 10, between=between, step_graph=True, **kw))
 
@@ -181,14 +198,15 @@ def test_ensemble_one_graph_matches_members_alone():
 def test_kept_residual_matches_recomputed(step_graph):
     """Pass 0 of the mixed form reads r(p) from the FP64 residual kept from
     the last pass, corrected face by face where calcPermeability changed T.
-    Re-uploading the pressure before every step discards the kept residual,
+    Replacing the pressure (different values, then its own again) before
+    every step discards the kept residual,
     so that run recomputes r(p) in full: the two runs must take the same
     decisions and agree to rounding."""
     case = _case(seed=12)
     kw = dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=step_graph)
 
     def reupload(sim):
-        sim.upload(None, None, None, sim.download("pressure"))
+        _replace(sim, "pressure")
 
     from conftest import rel_l2
     kept = _run(case, 10, **kw)
@@ -209,7 +227,7 @@ def test_kept_residual_matches_recomputed(step_graph):
 @pytest.mark.parametrize("step_graph", [False, True])
 def test_quiescent_bricks_skipped_exactly(step_graph):
     """The fused update skips bricks that were all copies, with their
-    neighbours, in the last update.  Re-uploading the concentration before
+    neighbours, in the last update.  Replacing the concentration before
     every step discards that record, so that run classifies every brick: the
     two runs must agree (FP64 form, previous-pressure start, so nothing else
     differs between them)."""
@@ -217,7 +235,7 @@ def test_quiescent_bricks_skipped_exactly(step_graph):
     kw = dict(solver="fp64", rtol=1e-10, step_graph=step_graph)
 
     def reupload(sim):
-        sim.upload(None, None, sim.download("concent"), None)
+        _replace(sim, "concent")
 
     skip = _run(case, 12, **kw)
     full = _run(case, 12, between={s: reupload for s in range(2, 12)}, **kw)
