@@ -337,8 +337,69 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
 // copy through a dense staging buffer and is re-pitched on the device (block
 // = one row of nx+2 values): row-by-row 2D copies of 2 KB rows run far below
 // the link's bandwidth.
+// Host layout <-> pitched device field as a flat walk over 16-byte pairs of
+// the dense array (one row-major index e -> row e / w, column e % w), each
+// thread keeping four pairs in flight: the dense side is the caller's host
+// array when the device reaches it in place, where many outstanding requests
+// keep the link busy.  Needs a 16-byte aligned dense array.
+__device__ __forceinline__ long long pitched_of(const Grid& g, unsigned long long e, unsigned w) {
+    const unsigned long long r = e / w;
+    return g.at(0, 0, 0) + (long long)r * g.P + (long long)(e - r * w);
+}
+
+// in: writes only the values that differ bitwise from the device copy and
+// flags *changed if any did
+__global__ void __launch_bounds__(256) k_dense_in(Grid g, const double2* __restrict__ src,
+                                                  double* __restrict__ dst, long long G, int* changed) {
+    const unsigned w = g.nx + 2;
+    const long long npair = G >> 1, stride = (long long)gridDim.x * blockDim.x;
+    int chg = 0;
+    auto put = [&](long long o, double v) {
+        if (__double_as_longlong(dst[o]) != __double_as_longlong(v)) {
+            dst[o] = v;
+            chg = 1;
+        }
+    };
+    for (long long q0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; q0 < npair; q0 += 4 * stride) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q0 + u * stride < npair) v[u] = src[q0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long q = q0 + u * stride;
+            if (q >= npair) break;
+            put(pitched_of(g, 2ull * q, w), v[u].x);
+            put(pitched_of(g, 2ull * q + 1, w), v[u].y);
+        }
+    }
+    if ((G & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        put(pitched_of(g, G - 1, w), reinterpret_cast<const double*>(src)[G - 1]);
+    if (__syncthreads_or(chg) && threadIdx.x == 0) *changed = 1;
+}
+
+__global__ void __launch_bounds__(256) k_dense_out(Grid g, const double* __restrict__ src,
+                                                   double2* __restrict__ dst, long long G) {
+    const unsigned w = g.nx + 2;
+    const long long npair = G >> 1, stride = (long long)gridDim.x * blockDim.x;
+    for (long long q0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; q0 < npair; q0 += 4 * stride) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long q = q0 + u * stride;
+            if (q < npair) v[u] = make_double2(src[pitched_of(g, 2ull * q, w)], src[pitched_of(g, 2ull * q + 1, w)]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q0 + u * stride < npair) dst[q0 + u * stride] = v[u];
+    }
+    if ((G & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        reinterpret_cast<double*>(dst)[G - 1] = src[pitched_of(g, G - 1, w)];
+}
+
 // Host layout -> pitched device field, writing only the values that differ
-// bitwise from the device copy and flagging *changed if any did.
+// bitwise from the device copy and flagging *changed if any did (row per
+// block: any alignment).
 __global__ void k_repitch_in(Grid g, const double* __restrict__ src, double* __restrict__ dst, int* changed) {
     const int w = g.nx + 2;
     const long long row = blockIdx.x;
@@ -417,8 +478,13 @@ static int copy_field_in(wpf_handle* h, double* dst, const double* src, int* cha
         WPF_CUDA(cudaMemcpyAsync(h->staging, src, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         from = h->staging;
     }
-    WPF_LAUNCH(h, KC_OTHER, k_repitch_in<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
-        g, from, dst, changed));
+    const long long G = (long long)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    if (((uintptr_t)from & 15u) == 0)
+        WPF_LAUNCH(h, KC_OTHER, k_dense_in<<<(unsigned)h->nsm * 8, 256, 0, h->stream>>>(
+            g, reinterpret_cast<const double2*>(from), dst, G, changed));
+    else
+        WPF_LAUNCH(h, KC_OTHER, k_repitch_in<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+            g, from, dst, changed));
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
@@ -426,8 +492,13 @@ static int copy_field_in(wpf_handle* h, double* dst, const double* src, int* cha
 static int copy_field_out(wpf_handle* h, double* dst, const double* src) {
     const Grid& g = h->g;
     if (double* hd = static_cast<double*>(const_cast<void*>(host_direct(h, dst)))) {   // write in place
-        WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
-            g, src, hd, 0));
+        const long long G = (long long)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+        if (((uintptr_t)hd & 15u) == 0)
+            WPF_LAUNCH(h, KC_OTHER, k_dense_out<<<(unsigned)h->nsm * 8, 256, 0, h->stream>>>(
+                g, src, reinterpret_cast<double2*>(hd), G));
+        else
+            WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+                g, src, hd, 0));
         WPF_CUDA(cudaGetLastError());
         return WPF_OK;
     }
