@@ -47,7 +47,7 @@
 namespace wpf {
 
 constexpr double COARSE_SCALE = 0.5;
-constexpr int SX = 32, SY = 8, SZC = 32;   // sweep tile (x, y) and z chunk
+constexpr int SX = 32, SY = 8;   // sweep tile (x, y); the z chunk is chosen per level (sweep_chunk)
 constexpr int FX = SX + 4, FY = SY + 4;    // shared footprint: tile + 2-cell ring
 
 // ---------------------------------------------------------------------------
@@ -411,7 +411,7 @@ __device__ __forceinline__ R offsum(const R* __restrict__ cx, const R* __restric
 
 // ---------------------------------------------------------------------------
 // Pipelined red-black sweep for the large levels.  Block = 32x8 threads, tile
-// = 32x8 cells of a plane, z chunk of SZC planes.  Shared memory holds NSLOT
+// = 32x8 cells of a plane, z chunk of szc planes.  Shared memory holds NSLOT
 // plane slots; each slot carries x on the tile + 2-cell ring and the
 // couplings / 1/diag / b on the tile + 1-cell ring, filled by cp.async
 // (4- or 8-byte async copies, zero-filled outside the halo box) two planes
@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
                                                          const R* __restrict__ xc, Grid gc,
                                                          double* dot,
                                                          const __grid_constant__ SweepMaps maps,
-                                                         int* err) {
+                                                         int* err, int szc) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t mbar[NSLOT];
     // slots on a 128-byte boundary whatever the dynamic window's base (the
@@ -539,8 +539,8 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     constexpr int MAXC = (NCH + NT - 1) / NT;         // chunks per thread
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * SX + tx;
     const int i0 = 1 + blockIdx.x * SX, j0 = 1 + blockIdx.y * SY;
-    const int k0 = 1 + blockIdx.z * SZC;
-    const int k1 = min(g.nz, k0 + SZC - 1);
+    const int k0 = 1 + blockIdx.z * szc;
+    const int k1 = min(g.nz, k0 + szc - 1);
     R dacc = 0;
 
     // this thread's chunks: source array, row offset (plane 0), smem offset, row j
@@ -1212,8 +1212,8 @@ static int build_hierarchy(wpf_handle* h, Hierarchy<R>& H) {
     return WPF_OK;
 }
 
-static dim3 sweep_grid(const Grid& g) {
-    return dim3((g.nx + SX - 1) / SX, (g.ny + SY - 1) / SY, (g.nz + SZC - 1) / SZC);
+static dim3 sweep_grid(const Grid& g, int szc) {
+    return dim3((g.nx + SX - 1) / SX, (g.ny + SY - 1) / SY, (g.nz + szc - 1) / szc);
 }
 
 template <typename R>
@@ -1291,6 +1291,42 @@ static bool ensure_maps(Hierarchy<R>& H, int l) {
 
 // One sweep of level l from `in` to `out` (the TMA-staged kernel unless the
 // maps are unavailable or the caller asked for the cp.async one).
+// z chunk of the pipelined sweep on grid g.  A block marches szc + 5 planes
+// (two staged below the chunk, the pipeline's fill and drain above) and the
+// blocks run in waves of (resident blocks per SM) x SMs, so the chunk count
+// nzc is the one that minimises  waves(tiles * nzc) * (ceil(nz / nzc) + 5):
+// at 256^3 seven chunks of 37 planes (1792 blocks, 3.9 waves) rather than
+// eight of 32 (2048 blocks, 4.5 waves).
+template <typename R>
+static int sweep_chunk(const wpf_handle* h, const Grid& g) {
+    static int per_sm = 0;   // resident sweep blocks per SM (shared memory bound)
+    if (!per_sm) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep_async<R, false, true>, SX * SY,
+                                                          sweep_smem<R>()) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 1;
+        }
+        per_sm = b;
+    }
+    const long long resident = (long long)per_sm * h->nsm;
+    const long long tiles = (long long)((g.nx + SX - 1) / SX) * ((g.ny + SY - 1) / SY);
+    int best = g.nz, best_nzc = 1;
+    long long best_cost = -1;
+    for (int nzc = 1; nzc <= g.nz && nzc <= 64; ++nzc) {
+        const int szc = (g.nz + nzc - 1) / nzc;
+        const int real = (g.nz + szc - 1) / szc;
+        const long long waves = (tiles * real + resident - 1) / resident;
+        const long long cost = waves * (szc + 5);
+        if (best_cost < 0 || cost < best_cost || (cost == best_cost && real < best_nzc)) {
+            best_cost = cost;
+            best = szc;
+            best_nzc = real;
+        }
+    }
+    return best;
+}
+
 template <typename R>
 static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool zero, const R* in, R* out,
                          int c0, const R* xc, const Grid& gc, double* dot) {
@@ -1302,18 +1338,20 @@ static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool ze
     const SweepMaps& m = H.tm[l][in == L.x ? 1 : 0];
     int* err = reinterpret_cast<int*>(h->dsc + S_KERR);
     const size_t sm = sweep_smem<R>();
+    const int szc = sweep_chunk<R>(h, g);
+    const dim3 gr = sweep_grid(g, szc);
     if (tma && zero)
-        WPF_LAUNCH(h, cls, k_sweep_async<R, true, true><<<sweep_grid(g), sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+        WPF_LAUNCH(h, cls, k_sweep_async<R, true, true><<<gr, sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
     else if (tma)
-        WPF_LAUNCH(h, cls, k_sweep_async<R, false, true><<<sweep_grid(g), sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+        WPF_LAUNCH(h, cls, k_sweep_async<R, false, true><<<gr, sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
     else if (zero)
-        WPF_LAUNCH(h, cls, k_sweep_async<R, true, false><<<sweep_grid(g), sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+        WPF_LAUNCH(h, cls, k_sweep_async<R, true, false><<<gr, sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
     else
-        WPF_LAUNCH(h, cls, k_sweep_async<R, false, false><<<sweep_grid(g), sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err));
+        WPF_LAUNCH(h, cls, k_sweep_async<R, false, false><<<gr, sb, sm, s>>>(
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
 }
 
 template <typename R>
