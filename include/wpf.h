@@ -270,7 +270,7 @@ int wpf_ensemble_run(wpf_handle** members, int32_t n, int32_t itime0, int32_t ns
  * integer pipe (GB300 issues the hardware conversions on its narrow FP64
  * pipe): converts each of the n host values both ways on the current device
  * and counts, in *mismatches, the results that differ from the hardware
- * conversions (FP32-subnormal results flush to zero by design).            */
+ * conversions (arguments below 2^-126 in magnitude flush to zero by design). */
 int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatches);
 
 #ifdef __cplusplus

@@ -798,9 +798,10 @@ __global__ void k_check_conversions(const double* x, long long n, unsigned long 
         const float got = f64_to_f32(v);
         const unsigned ur = __float_as_uint(ref), ug = __float_as_uint(got);
         const unsigned ar = ur & 0x7fffffffu;
+        const unsigned vhi = (unsigned)__double2hiint(v) & 0x7fffffffu;
         bool ok;
         if (ar > 0x7f800000u) ok = (ug & 0x7fffffffu) > 0x7f800000u;                 // NaN
-        else if (ar != 0u && ar < 0x00800000u) ok = ug == (ur & 0x80000000u);        // FP32 subnormal: flushed
+        else if (vhi < 0x38100000u) ok = ug == (ur & 0x80000000u);                   // |x| < 2^-126: flushed
         else ok = ug == ur;
         if (!ok) ++nb;
         const float f = ref;

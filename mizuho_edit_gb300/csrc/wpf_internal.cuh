@@ -340,32 +340,45 @@ inline unsigned long long dkey_host(double v) {
 // GB300 issues the hardware FP64<->FP32 conversions on its narrow FP64 pipe, at
 // a fraction of even the FP64 FMA rate; the kernels that convert a field per
 // cell use these instead, built from the IEEE 754 binary64 / binary32
-// layouts.  f64_to_f32: round to nearest, ties to even, for every result in
-// FP32's normal range; results below 2^-126 in magnitude flush to zero,
-// overflow gives infinity, NaN stays NaN.  f32_to_f64: exact for normal
+// layouts.  f64_to_f32: round to nearest, ties to even, for every argument of
+// magnitude at least 2^-126 (FP32's normal range); smaller arguments flush to
+// zero, overflow gives infinity, NaN stays NaN.  f32_to_f64: exact for normal
 // numbers; FP32 subnormals flush to zero.
 __device__ __forceinline__ float f64_to_f32(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    unsigned long long a = b & 0x7fffffffffffffffull;
+    // 32-bit operations on the two halves only (64-bit integer arithmetic
+    // can also land on the FP64 pipe)
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ahi = hi & 0x7fffffffu;
     unsigned f;
-    if (a >= 0x47f0000000000000ull) {          // |x| >= 2^128, Inf, NaN
-        f = a > 0x7ff0000000000000ull ? 0x7fc00000u : 0x7f800000u;
-    } else if (a < 0x3810000000000000ull) {    // |x| < 2^-126
+    if (ahi >= 0x47f00000u) {                  // |x| >= 2^128, Inf, NaN
+        f = (ahi > 0x7ff00000u || (ahi == 0x7ff00000u && lo)) ? 0x7fc00000u : 0x7f800000u;
+    } else if (ahi < 0x38100000u) {            // |x| < 2^-126
         f = 0u;
     } else {
-        a += 0x0fffffffull + ((a >> 29) & 1ull);   // round the 29 dropped bits, ties to even
-        f = (unsigned)((a >> 29) - (896ull << 23));   // rebias the exponent (1023 -> 127)
+        // exponent rebiased (1023 -> 127), the top 23 mantissa bits, and the
+        // 29 dropped bits rounded to nearest, ties to even (a carry runs into
+        // the exponent, and to Inf past the largest finite value)
+        f = ((ahi - 0x38000000u) << 3) | (lo >> 29);
+        const unsigned rem = lo & 0x1fffffffu;
+        f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
     }
-    return __uint_as_float(f | (unsigned)(b >> 32 & 0x80000000ull));
+    return __uint_as_float(f | (hi & 0x80000000u));
 }
 __device__ __forceinline__ double f32_to_f64(float x) {
     const unsigned u = __float_as_uint(x);
     const unsigned a = u & 0x7fffffffu;
-    unsigned long long b;
-    if (a >= 0x7f800000u) b = 0x7ff0000000000000ull | ((unsigned long long)(a & 0x7fffffu) << 29);
-    else if (a < 0x00800000u) b = 0ull;
-    else b = ((unsigned long long)a << 29) + (896ull << 52);
-    return __longlong_as_double((long long)(b | ((unsigned long long)(u & 0x80000000u) << 32)));
+    unsigned hi, lo;
+    if (a >= 0x7f800000u) {                    // Inf, NaN (payload kept)
+        hi = 0x7ff00000u | ((a & 0x7fffffu) >> 3);
+        lo = a << 29;
+    } else if (a < 0x00800000u) {              // zero and FP32 subnormals
+        hi = 0u;
+        lo = 0u;
+    } else {
+        hi = (a >> 3) + 0x38000000u;
+        lo = a << 29;
+    }
+    return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
 }
 template <typename R>
 __device__ __forceinline__ R from_f64(double x);

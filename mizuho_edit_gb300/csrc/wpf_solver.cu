@@ -213,6 +213,7 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    double* dsc, const double* __restrict__ rk_in = nullptr) {
     double rr1 = 0.0, rr0 = 0.0, bb = 0.0, rw = 0.0, ww = 0.0;
     R rr1r = 0, rwr = 0, wwr = 0;   // the same sums in R (with D)
+    float rr0f = 0.f;               // ||r(p)||^2 in FP32 on the kept path (only the fallback test reads it)
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                 // r(p) kept from the last residual pass, corrected face by
                 // face for the new T: FP64 work only next to a Dirichlet cell
                 r0 = rk_in[n];
-                if (dm || q != 0.0)
+                if (dm || (qterm && q != 0.0))
                     bref_add(pr[n + 1], pr[n - 1], pr[n + sy], pr[n - sy], pr[n + sz], pr[n - sz], Tx[n],
                              Tx[n - 1], Ty[n], Ty[n - sy], Tz[n], Tz[n - sz]);
             } else {
@@ -279,9 +280,15 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
             rr1 += r1 * r1;
         }
         dnew[n] = e;
-        rr0 += r0 * r0;
+        if (KEPT) {
+            const float f0 = f64_to_f32(r0);
+            rr0f = fmaf(f0, f0, rr0f);
+        } else {
+            rr0 += r0 * r0;
+        }
     }
     rr1 += (double)rr1r;
+    rr0 += (double)rr0f;
     rw += (double)rwr;
     ww += (double)wwr;
     block_add(rr1, dsc + S_RR64);

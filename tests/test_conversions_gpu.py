@@ -1,7 +1,7 @@
 """The FP64 <-> FP32 conversions the kernels perform on the integer pipe
 agree with the hardware conversions: round to nearest even into FP32 over
 the whole FP32 normal range (ties, carries into the exponent, the overflow
-boundary), Inf and NaN, and exact FP32 -> FP64; FP32-subnormal results flush
+boundary), Inf and NaN, and exact FP32 -> FP64; arguments below 2^-126 flush
 to zero by design."""
 import ctypes as C
 
