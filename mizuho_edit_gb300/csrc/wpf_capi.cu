@@ -415,15 +415,12 @@ __global__ void k_repitch_in(Grid g, const double* __restrict__ src, double* __r
     if (__syncthreads_or(chg) && threadIdx.x == 0) *changed = 1;
 }
 
-__global__ void k_repitch(Grid g, const double* __restrict__ src, double* __restrict__ dst,
-                          int to_pitched) {
+// Pitched device field -> host layout, row per block (any alignment).
+__global__ void k_repitch_out(Grid g, const double* __restrict__ src, double* __restrict__ dst) {
     const int w = g.nx + 2;
     const long long row = blockIdx.x;
     const long long dense = row * w, pitched = g.at(0, 0, 0) + row * g.P;
-    for (int i = threadIdx.x; i < w; i += blockDim.x) {
-        if (to_pitched) dst[pitched + i] = src[dense + i];
-        else dst[dense + i] = src[pitched + i];
-    }
+    for (int i = threadIdx.x; i < w; i += blockDim.x) dst[dense + i] = src[pitched + i];
 }
 
 // FP32 dense interior copies of pressure, phase, concentration and the cell
@@ -497,16 +494,16 @@ static int copy_field_out(wpf_handle* h, double* dst, const double* src) {
             WPF_LAUNCH(h, KC_OTHER, k_dense_out<<<(unsigned)h->nsm * 8, 256, 0, h->stream>>>(
                 g, src, reinterpret_cast<double2*>(hd), G));
         else
-            WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
-                g, src, hd, 0));
+            WPF_LAUNCH(h, KC_OTHER, k_repitch_out<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+                g, src, hd));
         WPF_CUDA(cudaGetLastError());
         return WPF_OK;
     }
     int rc = ensure_staging(h);
     if (rc) return rc;
     const size_t G = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
-    WPF_LAUNCH(h, KC_OTHER, k_repitch<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
-        g, src, h->staging, 0));
+    WPF_LAUNCH(h, KC_OTHER, k_repitch_out<<<(unsigned)((g.ny + 2) * (g.nz + 2)), 128, 0, h->stream>>>(
+        g, src, h->staging));
     WPF_CUDA(cudaGetLastError());
     WPF_CUDA(cudaMemcpyAsync(dst, h->staging, G * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return WPF_OK;

@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
     // in FP64 for the next solve's pass 0
     if (skip && *skip) return;
     double rr = 0.0, bb = 0.0;
+    R rrr = 0;
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
@@ -126,10 +127,15 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
                 bb += bref * bref;
             }
         }
-        rout[n] = from_f64<R>(r);
+        const R rr_ = from_f64<R>(r);
+        rout[n] = rr_;
         if (rk_out) rk_out[n] = r;
-        rr += r * r;
+        // the FP32 form squares the rounded residual in FP32 (FP64 across
+        // threads: ~1e-6 relative in the norm, none of the FP64 pipe)
+        if (sizeof(R) == 4) rrr += rr_ * rr_;
+        else rr += r * r;
     }
+    rr += (double)rrr;
     block_add(rr, dsc + S_RR64);
     if (want_b) block_add(bb, dsc + S_BB64);
 }
