@@ -293,8 +293,8 @@ def run_ours(args):
     # least 2^23 cells runs the one-pass pipelined sweep, whose algorithmic
     # bytes per cell (FP32) are: couplings cx,cy,cz (12 B) + 1/diag (4 B) +
     # b (4 B) + the input x (4 B) + the output x (4 B) = 28 B; the zero-guess
-    # first sweep of a cycle reads no input x (24 B); the first post-sweep also
-    # reads the coarse correction (1/8 cell, 0.5 B).  Four sweeps per cycle
+    # first sweep of a cycle reads no input x (24 B); the coarse correction is
+    # a separate prolongation pass before the post-sweeps.  Four sweeps per cycle
     # (nu = 2 on each side).  Smaller finest levels run two half-sweep
     # kernels: 20 B/cell each (12 B couplings + 2 B other colour + 6 B b,
     # 1/diag, new x of this colour), 12 B for the zero-guess one.
@@ -303,7 +303,7 @@ def run_ours(args):
     smooth_ms = float(kms[KC_SMOOTH0])
     if ncell >= (1 << 23):
         cycles = cnt // (2 * nu)
-        smooth_bytes = (cycles * 24.0 + (cnt - cycles) * 28.0 + cycles * 0.5) * ncell
+        smooth_bytes = (cycles * 24.0 + (cnt - cycles) * 28.0) * ncell
         kname, per_cell = "k_sweep_async<float> (finest level)", 28
     else:
         n_first = cnt // (4 * nu)

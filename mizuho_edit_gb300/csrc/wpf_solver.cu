@@ -507,8 +507,11 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// ZERO: xin is zero (first pre-smoothing sweep).  xc != null: prolongation
-// x += x_{l+1}(parent) fused into the staged x.  dot != null: accumulate b.xout.
+// ZERO: xin is zero (first pre-smoothing sweep).  dot != null: accumulate
+// b.xout.  (The coarse correction before the first post-sweep is a separate
+// k_prolong pass on the input buffer: added here, per thread on its staged x
+// chunks with scattered reads of the coarse level, it made that sweep 45 %
+// slower than the others for less than half that as a separate pass.)
 // Every staged row is a 16-byte aligned window of WX elements starting at
 // i = i0 - 4 (XOFF and the pitches make at(i0-4, j, k) a multiple of 4
 // elements).  TMA: one thread stages a plane with five or six bulk-tensor
@@ -524,7 +527,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
                                                          const R* __restrict__ b,
                                                          const R* __restrict__ xin,
                                                          R* __restrict__ xout, int c0,
-                                                         const R* __restrict__ xc, Grid gc,
                                                          double* dot,
                                                          const __grid_constant__ SweepMaps maps,
                                                          int* err, int szc) {
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     // this thread's chunks: source array, row offset (plane 0), smem offset, row j
     const R* csrc[MAXC];
     long long coff[MAXC];
-    int csm[MAXC], cj[MAXC], ci[MAXC];
+    int csm[MAXC];
     bool cx_ok[MAXC], cis_x[MAXC];
 #pragma unroll
     for (int s = 0; s < MAXC; ++s) {
@@ -567,8 +569,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         csrc[s] = nullptr;
         coff[s] = 0;
         csm[s] = 0;
-        cj[s] = -1;
-        ci[s] = 0;
         cx_ok[s] = false;
         cis_x[s] = false;
         if (q >= NCH) continue;
@@ -587,8 +587,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         }
         const int e0 = i0 - 4 + ch * EPC;
         csrc[s] = src;
-        cj[s] = j;
-        ci[s] = e0;
         cx_ok[s] = j >= 0 && j <= g.ny + 1 && e0 <= g.nx + 1;
         coff[s] = XOFF + (long long)j * g.P + e0;
         csm[s] = slot_row_offset<R>(srow) + ch * EPC;
@@ -645,23 +643,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         if (!wait_ok) return;
         if (!mbar_wait_bounded(&mbar[slot_index(k)], (unsigned)(((k - (k0 - 2)) / NSLOT) & 1))) wait_ok = false;
     };
-    // after plane k has landed: add the coarse correction to this thread's x chunks
-    auto correct = [&](int k) {
-        if (ZERO || !xc || k < 1 || k > g.nz) return;
-        R* base = slot_base(k);
-        const int K = (k + 1) >> 1;
-#pragma unroll
-        for (int s = 0; s < MAXC; ++s) {
-            if (!cis_x[s] || cj[s] < 1 || cj[s] > g.ny) continue;
-            const int J = (cj[s] + 1) >> 1;
-#pragma unroll
-            for (int e = 0; e < EPC; ++e) {
-                const int i = ci[s] + e;
-                if (i >= 1 && i <= g.nx) base[csm[s] + e] += xc[gc.at((i + 1) >> 1, J, K)];
-            }
-        }
-    };
-    const bool corrects = !ZERO && xc != nullptr;   // this sweep adds the coarse correction
     // Updated value of the cell at slot column w, slot row c (R1 row) of plane
     // k; neighbours = false when they are all known to be zero (first colour
     // of the zero-guess sweep).
@@ -726,7 +707,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
     } else {
         cp_async_wait<2>();                   // planes k0-2 .. k0+1 landed
     }
-    for (int k = k0 - 2; k <= k0 + 1; ++k) correct(k);
     __syncthreads();
     first_colour(k0 - 1, slot(k0 - 1), slot(k0 - 2), slot(k0));
     __syncthreads();
@@ -743,9 +723,7 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
         // whose last readers (second colour of k-2, write-out of k-3) and
         // fenced writers finished before the last barrier.  Every thread
         // waits on the plane's mbarrier itself, which makes the landed copies
-        // visible to it; only the coarse correction, written by each thread
-        // into its own chunks of plane k+2 and read by the others, takes a
-        // barrier more.
+        // visible to it.
         for (int k = k0; k <= k1 + 1; ++k) {
             const int skm1 = sk == 0 ? NSLOT - 1 : sk - 1;
             const int skm2 = skm1 == 0 ? NSLOT - 1 : skm1 - 1;
@@ -755,10 +733,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             if (k <= k1) {
                 issue(k + 4);
                 landed(k + 2);
-                if (corrects) {
-                    correct(k + 2);
-                    __syncthreads();
-                }
             }
             if (k - 2 >= k0) write_out(k - 2, slots[skm2]);
             if (k <= k1) first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
@@ -773,7 +747,6 @@ __global__ void __launch_bounds__(SX * SY) k_sweep_async(Grid g, const R* __rest
             const int skp2 = skp1 == NSLOT - 1 ? 0 : skp1 + 1;
             issue(k + 4);                     // the slot of plane k-3, idle since k-2
             cp_async_wait<2>();               // plane k+2 landed
-            correct(k + 2);
             __syncthreads();
             if (k > k0) write_out(k - 1, slots[skm1]);
             first_colour(k + 1, slots[skp1], slots[sk], slots[skp2]);
@@ -1342,7 +1315,7 @@ static int sweep_chunk(const wpf_handle* h, const Grid& g) {
 
 template <typename R>
 static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool zero, const R* in, R* out,
-                         int c0, const R* xc, const Grid& gc, double* dot) {
+                         int c0, double* dot) {
     Level<R>& L = H.lv[l];
     const Grid& g = L.g;
     cudaStream_t s = h->stream;
@@ -1355,16 +1328,16 @@ static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool ze
     const dim3 gr = sweep_grid(g, szc);
     if (tma && zero)
         WPF_LAUNCH(h, cls, k_sweep_async<R, true, true><<<gr, sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, dot, m, err, szc));
     else if (tma)
         WPF_LAUNCH(h, cls, k_sweep_async<R, false, true><<<gr, sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, dot, m, err, szc));
     else if (zero)
         WPF_LAUNCH(h, cls, k_sweep_async<R, true, false><<<gr, sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, dot, m, err, szc));
     else
         WPF_LAUNCH(h, cls, k_sweep_async<R, false, false><<<gr, sb, sm, s>>>(
-            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, xc, gc, dot, m, err, szc));
+            g, L.cx, L.cy, L.cz, L.idiag, L.b, in, out, c0, dot, m, err, szc));
 }
 
 template <typename R>
@@ -1406,7 +1379,7 @@ static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, l
         for (int it = 0; it < nu; ++it) {
             const R* in = buf[(it + 1) & 1];
             R* out = buf[it & 1];
-            launch_sweep(h, H, l, cls, it == 0, in, out, 0, (const R*)nullptr, g, nullptr);
+            launch_sweep(h, H, l, cls, it == 0, in, out, 0, nullptr);
         }
         const R* pre_end = buf[(nu - 1) & 1];
         WPF_LAUNCH(h, KC_MGREST, k_resid_restrict<R><<<cell_grid(C.g.nx, C.g.ny, C.g.nz), cell_block(), 0, s>>>(
@@ -1414,12 +1387,14 @@ static void cycle_level(wpf_handle* h, Hierarchy<R>& H, int l, int lb, int nu, l
         cycle_level(h, H, l + 1, lb, nu, big, wfrom, nullptr, need_dot);
         for (int it = 0; it < nu; ++it) {
             const int w = nu + it;   // sweep number in the cycle: writes buf[w & 1]
-            const R* in = buf[(w + 1) & 1];
+            R* in = buf[(w + 1) & 1];
             R* out = buf[w & 1];
             const bool last0 = (l == 0 && it == nu - 1 && rz);
             if (last0) need_dot = false;
-            launch_sweep(h, H, l, cls, false, in, out, 1, it == 0 ? (const R*)C.x : nullptr, C.g,
-                         last0 ? rz : nullptr);
+            if (it == 0)   // the coarse correction, into the first post-sweep's input
+                WPF_LAUNCH(h, KC_MGREST, k_prolong<R><<<cell_grid(g.nx, g.ny, g.nz), cell_block(), 0, s>>>(
+                    g, C.g, L.idiag, in, C.x));
+            launch_sweep(h, H, l, cls, false, in, out, 1, last0 ? rz : nullptr);
         }
         return;
     }

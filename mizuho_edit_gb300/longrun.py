@@ -108,7 +108,7 @@ def run(n: int, steps: int, solver: str, extrapolate: bool, log_var: float, corr
             cnt = int(kcnt[3])
             if ms["smooth_l0"] > 0 and cnt:
                 cyc = cnt // 4
-                b = (cyc * 24.0 + (cnt - cyc) * 28.0 + cyc * 0.5) * cells
+                b = (cyc * 24.0 + (cnt - cyc) * 28.0) * cells
                 out["smooth_l0_gbs"] = b / (ms["smooth_l0"] / 1e3) / 1e9
             if ms["apply"] > 0:
                 out["apply_gbs"] = int(kcnt[5]) * 32.0 * cells / (ms["apply"] / 1e3) / 1e9
