@@ -101,6 +101,21 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: every rank's replica finishes within it."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, steps: int, ms: float) -> float:
+    """Whole-job time-steps/s: every rank advances its own replica `steps`
+    steps in the (max-over-ranks) time `ms` (weak scaling, replicas only)."""
+    return world * steps / (ms / 1000.0)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -280,13 +295,10 @@ def run_ours(args):
             sim.step()
     L.wpf_kernel_times(sim.h, kms, kcnt, NK)
     capi.check(L.wpf_set_kernel_timing(sim.h, 0), "timing")
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, world)
     n = args.n
     ncell = n ** 3
-    value = world * args.steps / (ms_max / 1000.0)
+    value = job_rate(world, args.steps, ms_max)
 
     # roofline of the finest-level red-black Gauss-Seidel smoother (the
     # largest share of the step in the launch list).  A finest level of at
@@ -398,13 +410,10 @@ def learned_pass(args, case, world):
         stats = [sim.step() for _ in range(args.steps)]
         e1.record(stream)
         torch.cuda.synchronize()
-        t = torch.tensor([e0.elapsed_time(e1)], device="cuda")
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world)
         learned.attach(sim, None)
     net.close()
-    return {"value": world * args.steps / (ms / 1000.0), "unit": "time-steps/s",
+    return {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
             "ms_per_step": ms / args.steps,
             "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
             "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
@@ -436,11 +445,8 @@ def plain_fp64_pass(args, case, world):
         stats = [sim.step() for _ in range(args.steps)]
         e1.record(stream)
         torch.cuda.synchronize()
-        t = torch.tensor([e0.elapsed_time(e1)], device="cuda")
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    return {"value": world * args.steps / (ms / 1000.0), "unit": "time-steps/s",
+        ms = max_over_ranks(e0.elapsed_time(e1), world)
+    return {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
             "ms_per_step": ms / args.steps,
             "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
             "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
@@ -491,13 +497,10 @@ def e2e_pass(args, sim, stream, world):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     for ptr, _ in bufs.values():
         L.wpf_host_free(ptr)
-    return {"value": world * args.steps / (ms / 1000.0), "unit": "time-steps/s",
+    return {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
             "h2d_bytes_per_step": 3 * G * 8, "d2h_bytes_per_step": 3 * G * 8,
             "path": "wpf_upload + wpf_step + wpf_download per step, pinned host buffers"}
 
