@@ -121,6 +121,8 @@ static void free_all(wpf_handle* h) {
     if (h->gctl) cudaFree(h->gctl);
     if (h->gctl_host) cudaFreeHost(h->gctl_host);
     if (h->gdsc_host) cudaFreeHost(h->gdsc_host);
+    if (h->split_graph) cudaGraphDestroy(h->split_graph);
+    if (h->cap_split) cudaStreamDestroy(h->cap_split);
     if (h->cap_side) cudaStreamDestroy(h->cap_side);
     if (h->cap_fork) cudaEventDestroy(h->cap_fork);
     if (h->cap_join) cudaEventDestroy(h->cap_join);
