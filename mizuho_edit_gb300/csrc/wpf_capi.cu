@@ -259,6 +259,7 @@ int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o) {
     h->ws_hist = 0;          // a new solver starts a new increment history
     h->ws_h1 = h->ws_h2 = 0.0;
     h->rkeep_ok = false;
+    h->l0_inc_ok = false;
     if (!(h->opts.inner_rtol > 0 && h->opts.inner_rtol < 1)) h->opts.inner_rtol = 1e-4;
     if (h->opts.smooth_sweeps == 0) h->opts.smooth_sweeps = 2;
     return WPF_OK;
@@ -329,6 +330,7 @@ int wpf_set_wells(wpf_handle* h, const wpf_well* wells, int32_t nwell) {
     h->have_wells = true;
     h->ws_hist = 0;   // new boundary conditions: the increment history no longer applies
     h->rkeep_ok = false;
+    h->l0_inc_ok = false;   // the well flags enter the level-0 operator
     h->bact_ok = false;   // the well flags enter the update's classification
     step_graphs_drop(h);   // the step graphs bake in the well arrays
     return phys_set_dirichlet(h);

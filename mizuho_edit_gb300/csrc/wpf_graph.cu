@@ -229,6 +229,8 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     long long l0 = h->nlaunch;
     WPF_LAUNCH(h, KC_OTHER, k_step_begin<<<1, 32, 0, s>>>(c, h->dsc, dt_c, dt_a));
     const bool tc = h->t_current, tp = h->t_from_prev, kv = h->kf_valid, rko = h->rkeep_ok;
+    const bool l0ok = h->l0_inc_ok;
+    const int l0m = h->l0_mode;
     rc = phys_permeability(h, false);
     h->t_current = tc;
     h->t_from_prev = tp;
@@ -236,12 +238,15 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     if (!rc) rc = capture_split_beside(h);
     if (rc) {
         h->rkeep_ok = rko;
+        h->l0_inc_ok = l0ok;
         drop_split(h);
         return rc;
     }
     n->fixed += h->nlaunch - l0;
     rc = solve_capture(h, b, n);   // the solve and the fused update (reads rkeep_ok as set above)
     h->rkeep_ok = rko;
+    h->l0_inc_ok = l0ok;   // set when the graph has run (step_graph_finish)
+    h->l0_mode = l0m;
     drop_split(h);
     if (rc) return rc;
     l0 = h->nlaunch;
@@ -304,6 +309,8 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     h->t_current = false;
     // every graph step ends on a plain residual pass of the final pressure
     h->rkeep_ok = h->rkeep && h->opts.mode == WPF_SOLVER_MIXED && c.status != WPF_ERR_NONFINITE;
+    h->l0_inc_ok = h->l0mark != nullptr;   // the step rebuilt the level-0 operator
+    h->l0_mode = h->opts.mode;
     const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter;
     h->nlaunch += launches;
     int rc = c.status;
@@ -350,6 +357,8 @@ void step_graph_key(const wpf_handle* h, const void** k) {
     k[6] = (h->t_from_prev && h->rkeep && h->rkeep_ok) ? h->rkeep : nullptr;
     // the update skips the bricks that were quiescent in the last update
     k[7] = h->bact_ok ? h->bact[0] : nullptr;
+    // the level-0 build rebuilds only the cells of recomputed faces
+    k[8] = (h->t_from_prev && l0_incremental(h)) ? h->l0mark : nullptr;
 }
 
 // Upload the increment step sizes when the host-driven path changed them.

@@ -138,7 +138,7 @@ int gb_handle(GraphBuilder& b, cudaGraphConditionalHandle* hd);
 int gb_cond(GraphBuilder& b, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hd,
             GraphBuilder* body);
 
-constexpr int STEP_KEY = 8;   // buffer pointers and modes a captured step depends on
+constexpr int STEP_KEY = 9;   // buffer pointers and modes a captured step depends on
 constexpr int BRICK_X = 32, BRICK_Y = 4, BRICK_Z = 2;   // fused-update bricks (one RB-thread block)
 
 // Kernels launched per step by a captured device-resident step:
@@ -204,6 +204,14 @@ struct wpf_handle {
     // read as r(p) by the next solve's pass 0.  rkeep_ok: it matches p and T.
     double* rkeep;
     bool rkeep_ok;
+    // level-0 operator kept up to date cell by cell: calcPermeability's
+    // incremental form marks both cells of every face it recomputes
+    // (l0mark), and the next level-0 build rebuilds only the marked cells and
+    // clears them.  l0_inc_ok: the level-0 arrays of the l0_mode hierarchy
+    // match T except at the marked cells.
+    uint8_t* l0mark;
+    bool l0_inc_ok;
+    int l0_mode;
     // extrapolated warm start (WPF_SOLVER_EXTRAPOLATE): the pressure increments
     // of the last two solves (ws[0] newest) and this solve's (ws[2]), FP32
     float* ws[3];
@@ -548,6 +556,8 @@ void update_advance_bricks(wpf_handle* h); // after an update: its activity beco
 // capture the solve and the fused update (Dirichlet values .. new phase and
 // concentration) into b, in capture on entry and exit
 int solve_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
+// the next level-0 build may rebuild only the cells calcPermeability marked
+bool l0_incremental(const wpf_handle* h);
 // capture the classification half of the fused update (step slots reset,
 // k_update_split) on stream s (launches only)
 int phys_capture_split(wpf_handle* h, cudaStream_t s);

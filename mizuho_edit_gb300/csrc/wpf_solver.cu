@@ -348,10 +348,15 @@ __global__ void __launch_bounds__(RB) k_l0_coeffs(Grid g, const double* __restri
                                                   const uint8_t* __restrict__ fl,
                                                   R* __restrict__ cx, R* __restrict__ cy,
                                                   R* __restrict__ cz, R* __restrict__ diag,
-                                                  R* __restrict__ idiag, double* __restrict__ dsum) {
+                                                  R* __restrict__ idiag, double* __restrict__ dsum,
+                                                  uint8_t* __restrict__ mark) {
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
+        if (mark) {   // incremental: only the cells with a recomputed face
+            if (!mark[n]) continue;
+            mark[n] = 0;
+        }
         const bool live = !(fl[n] & F_DIR);
         const R tx = from_f64<R>(Tx[n]), ty = from_f64<R>(Ty[n]), tz = from_f64<R>(Tz[n]);
         cx[n] = (live && !(fl[n + 1] & F_DIR)) ? tx : (R)0;
@@ -1207,12 +1212,22 @@ static void free_hierarchy(Hierarchy<R>& H) {
 // The FP64 diagonal sums of the outer residual's diagonal-sum form (mixed form only).
 static double* resid_dsum(wpf_handle* h) { return h->opts.mode == WPF_SOLVER_MIXED ? h->dsum : nullptr; }
 
+// Whether the next level-0 build may rebuild only the marked cells.
+bool l0_incremental(const wpf_handle* h) {
+    return h->l0mark && h->l0_inc_ok && h->l0_mode == h->opts.mode;
+}
+
 template <typename R>
 static void build_level0(wpf_handle* h, Hierarchy<R>& H, cudaStream_t s) {
     const Grid& g = h->g;
     Level<R>& L0 = H.lv[0];
+    const bool inc = l0_incremental(h);
+    if (!inc && h->l0mark) cudaMemsetAsync(h->l0mark, 0, (size_t)g.total, s);
     WPF_LAUNCH(h, KC_COEF, k_l0_coeffs<R><<<row_blocks(h, g), RB, 0, s>>>(
-        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag, resid_dsum(h)));
+        g, h->T[0], h->T[1], h->T[2], h->flags, L0.cx, L0.cy, L0.cz, L0.diag, L0.idiag, resid_dsum(h),
+        inc ? h->l0mark : nullptr));
+    h->l0_inc_ok = h->l0mark != nullptr;
+    h->l0_mode = h->opts.mode;
 }
 
 template <typename R>
@@ -1617,6 +1632,11 @@ int solver_setup(wpf_handle* h) {
             if ((rc = dev_alloc(h, (void**)&h->ws[q], sizeof(float) * h->g.total))) return rc;
         h->ws_hist = 0;
     }
+    if (!h->l0mark) {
+        if ((rc = dev_alloc(h, (void**)&h->l0mark, (size_t)h->g.total))) return rc;
+        WPF_CUDA(cudaMemsetAsync(h->l0mark, 0, (size_t)h->g.total, h->stream));
+        h->l0_inc_ok = false;
+    }
     if (h->opts.mode == WPF_SOLVER_MIXED) {
         rc = alloc_hierarchy(h, h->h32);
         if (rc) return rc;
@@ -1644,6 +1664,9 @@ int solver_free(wpf_handle* h) {
     if (h->rkeep) cudaFree(h->rkeep);
     h->rkeep = nullptr;
     h->rkeep_ok = false;
+    if (h->l0mark) cudaFree(h->l0mark);
+    h->l0mark = nullptr;
+    h->l0_inc_ok = false;
     for (int q = 0; q < 3; ++q) {
         if (h->ws[q]) cudaFree(h->ws[q]);
         h->ws[q] = nullptr;

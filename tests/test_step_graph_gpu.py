@@ -242,3 +242,30 @@ def test_quiescent_bricks_skipped_exactly(step_graph):
     _same_fields(full[1], skip[1])
     for n, (a, b) in enumerate(zip(full[0], skip[0])):
         _same_stats(a, b, n)
+
+
+@pytest.mark.parametrize("step_graph", [False, True])
+def test_level0_rebuilt_incrementally(step_graph):
+    """The level-0 operator (FP32 couplings, diagonal, and the FP64 diagonal
+    sums of the mixed form's outer residual) is rebuilt only at the cells
+    whose faces calcPermeability recomputed.  Replacing the phase before
+    every step makes calcPermeability recompute every face and the level-0
+    build rebuild every cell (it also drops the kept residual, so the runs
+    agree to the solver tolerance, as in the kept-residual test): the
+    decisions must be equal and the fields agree.  A stale diagonal sum would
+    move the converged pressure by the change of T at the interface cells."""
+    case = _case(seed=14)
+    kw = dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=step_graph)
+
+    def reupload(sim):
+        _replace(sim, "phase")
+
+    from conftest import rel_l2
+    inc = _run(case, 12, **kw)
+    full = _run(case, 12, between={s: reupload for s in range(3, 12)}, **kw)
+    for k in FIELDS:
+        assert rel_l2(inc[1][k], full[1][k]) <= 1e-7, k
+    for n, (a, b) in enumerate(zip(full[0], inc[0])):
+        for key in SAME:
+            assert a[key] == b[key], (n, key, a[key], b[key])
+        assert abs(a["relres"] - b["relres"]) <= 1e-9, (n, a["relres"], b["relres"])
