@@ -127,7 +127,7 @@ static void free_all(wpf_handle* h) {
     if (h->cap_fork) cudaEventDestroy(h->cap_fork);
     if (h->cap_join) cudaEventDestroy(h->cap_join);
     double* d[] = {h->krock, h->phase, h->concent, h->pressure, h->phase_n, h->concent_n,
-                   h->T[0], h->T[1], h->T[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
+                   h->T[0], h->T[1], h->T[2], h->Tv[0], h->Tv[1], h->Tv[2], h->K0, h->Kf[0], h->Kf[1], h->Kf[2],
                    h->vel[0], h->vel[1], h->vel[2], h->dphasedt, h->dconcentdt, h->dir_val,
                    h->qterm, h->dsc, h->partials, h->staging};
     for (double* p : d)
@@ -205,9 +205,9 @@ int wpf_create(const wpf_params* p, wpf_handle** out) {
     if (!rc && cudaMallocHost((void**)&h->hsc, S_COUNT * sizeof(double)) != cudaSuccess)
         rc = WPF_ERR_CUDA;
     const size_t fb = sizeof(double) * h->g.total;
-    double** arrs[9] = {&h->krock, &h->phase, &h->concent, &h->pressure, &h->phase_n, &h->concent_n,
-                        &h->T[0], &h->T[1], &h->T[2]};
-    for (int a = 0; a < 9 && !rc; ++a) rc = dev_alloc(h, (void**)arrs[a], fb);
+    double** arrs[12] = {&h->krock, &h->phase, &h->concent, &h->pressure, &h->phase_n, &h->concent_n,
+                         &h->T[0], &h->T[1], &h->T[2], &h->Tv[0], &h->Tv[1], &h->Tv[2]};
+    for (int a = 0; a < 12 && !rc; ++a) rc = dev_alloc(h, (void**)arrs[a], fb);
     if (!rc) rc = dev_alloc(h, (void**)&h->flags, h->g.total);
     if (!rc) rc = dev_alloc(h, (void**)&h->dsc, S_COUNT * sizeof(double));
     if (!rc) rc = dev_alloc(h, (void**)&h->dphys, sizeof(Phys));
