@@ -123,6 +123,9 @@ static void free_all(wpf_handle* h) {
     if (h->gdsc_host) cudaFreeHost(h->gdsc_host);
     if (h->split_graph) cudaGraphDestroy(h->split_graph);
     if (h->cap_split) cudaStreamDestroy(h->cap_split);
+    if (h->cap_ws) cudaStreamDestroy(h->cap_ws);
+    if (h->cap_ws_fork) cudaEventDestroy(h->cap_ws_fork);
+    if (h->cap_ws_join) cudaEventDestroy(h->cap_ws_join);
     if (h->cap_side) cudaStreamDestroy(h->cap_side);
     if (h->cap_fork) cudaEventDestroy(h->cap_fork);
     if (h->cap_join) cudaEventDestroy(h->cap_join);

@@ -206,6 +206,11 @@ int step_graph_prepare(wpf_handle* h) {
         h->gctl_dirty = true;
     }
     if (!h->cap_split) WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_split, cudaStreamNonBlocking));
+    if (!h->cap_ws) {
+        WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_ws, cudaStreamNonBlocking));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->cap_ws_fork, cudaEventDisableTiming));
+        WPF_CUDA(cudaEventCreateWithFlags(&h->cap_ws_join, cudaEventDisableTiming));
+    }
     if (!h->cap_side) {
         WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_side, cudaStreamNonBlocking));
         WPF_CUDA(cudaEventCreateWithFlags(&h->cap_fork, cudaEventDisableTiming));
@@ -228,6 +233,9 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     if ((rc = gb_begin(b))) return rc;
     long long l0 = h->nlaunch;
     WPF_LAUNCH(h, KC_OTHER, k_step_begin<<<1, 32, 0, s>>>(c, h->dsc, dt_c, dt_a));
+    // the extrapolated start needs only the dt law's coefficients: it is
+    // built beside calcPermeability (HBM-bound beside FP64-bound)
+    if ((rc = ws_capture_early(h, &h->ws_early))) return rc;
     const bool tc = h->t_current, tp = h->t_from_prev, kv = h->kf_valid, rko = h->rkeep_ok;
     const bool l0ok = h->l0_inc_ok;
     const int l0m = h->l0_mode;
@@ -239,6 +247,7 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     if (rc) {
         h->rkeep_ok = rko;
         h->l0_inc_ok = l0ok;
+        h->ws_early = false;
         drop_split(h);
         return rc;
     }
@@ -247,6 +256,7 @@ int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n) {
     h->rkeep_ok = rko;
     h->l0_inc_ok = l0ok;   // set when the graph has run (step_graph_finish)
     h->l0_mode = l0m;
+    h->ws_early = false;
     drop_split(h);
     if (rc) return rc;
     l0 = h->nlaunch;

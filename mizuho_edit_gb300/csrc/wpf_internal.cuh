@@ -282,6 +282,11 @@ struct wpf_handle {
     // (calcPermeability) until it is added to the step graph
     cudaStream_t cap_split;
     cudaGraph_t split_graph;
+    // the extrapolated start's build, captured beside calcPermeability on
+    // cap_ws and joined before the pass-0 residual (ws_early: it was)
+    cudaStream_t cap_ws;
+    cudaEvent_t cap_ws_fork, cap_ws_join;
+    bool ws_early;
     cudaGraphNode_t split_deps[8];
     int nsplit_deps;
     static constexpr int MAX_STEP_GRAPHS = 12;
@@ -559,6 +564,10 @@ void update_advance_bricks(wpf_handle* h); // after an update: its activity beco
 int solve_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
 // the next level-0 build may rebuild only the cells calcPermeability marked
 bool l0_incremental(const wpf_handle* h);
+// capture the extrapolated start's build (e = wa d1 + wb d2 with the device
+// coefficients) on h->cap_ws, forked from h->stream; false if the solve has
+// no extrapolated start
+int ws_capture_early(wpf_handle* h, bool* launched);
 // capture the classification half of the fused update (step slots reset,
 // k_update_split) on stream s (launches only)
 int phys_capture_split(wpf_handle* h, cudaStream_t s);

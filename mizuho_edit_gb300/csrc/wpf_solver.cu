@@ -2014,8 +2014,14 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     if ((rc = gb_fork(h))) return rc;
     build_coarse(h, H, h->cap_side);
     if (ws_on) {
-        WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0], d,
-                                                                   &c->wa));
+        if (h->ws_early) {   // built beside calcPermeability
+            WPF_CUDA(cudaEventRecord(h->cap_ws_join, h->cap_ws));
+            WPF_CUDA(cudaStreamWaitEvent(s, h->cap_ws_join, 0));
+            h->ws_early = false;
+        } else {
+            WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
+                                                                       d, &c->wa));
+        }
         auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
         WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
             g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
@@ -2083,6 +2089,19 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     if ((rc = phys_capture_update(h, &c->dt, s, split_done))) return rc;
     WPF_CUDA(cudaEventRecordWithFlags(h->ev[3], s, cudaEventRecordExternal));
     cnt->fixed += h->nlaunch - l0;
+    return WPF_OK;
+}
+
+int ws_capture_early(wpf_handle* h, bool* launched) {
+    *launched = false;
+    if (!((h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && h->ws[0] && h->ws_e[0] && h->cap_ws)) return WPF_OK;
+    const Grid& g = h->g;
+    WPF_CUDA(cudaEventRecord(h->cap_ws_fork, h->stream));
+    WPF_CUDA(cudaStreamWaitEvent(h->cap_ws, h->cap_ws_fork, 0));
+    WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<row_blocks(h, g), RB, 0, h->cap_ws>>>(
+        g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0], h->dsc, &h->gctl->wa));
+    WPF_CUDA(cudaGetLastError());
+    *launched = true;
     return WPF_OK;
 }
 
