@@ -1,7 +1,7 @@
 """The CPU restatement of the warm-start network (oracle/net_oracle.py) pinned
 by its own mathematics: adjoint identities of the convolution pieces and
 finite differences of the loss through the whole U-Net (float64, no
-rounding).  These make it a trustworthy judge of the GPU gradients."""
+rounding).  These make it a trustworthy check of the GPU gradients."""
 import numpy as np
 import pytest
 
