@@ -9,7 +9,8 @@
 // and the step ends with two device-to-host copies (the control block and the
 // scalar slots) read after the one synchronisation of the step.  The kernels
 // are those of the host-driven step, so are the results; only the fused
-// update's classification runs beside the solve instead of after it.
+// update's classification and the extrapolated start's build run on side
+// branches (beside the solve and beside calcPermeability).
 //
 // A graph bakes in the buffers it was captured with; the step's ping-pong
 // buffers (phase, concentration and, with the extrapolated start, the three
