@@ -273,6 +273,14 @@ int wpf_ensemble_run(wpf_handle** members, int32_t n, int32_t itime0, int32_t ns
  * conversions (arguments below 2^-126 in magnitude flush to zero by design). */
 int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatches);
 
+/* Self-check of the reciprocal the harmonic means of calcPermeability use (a
+ * Newton-Raphson refinement of the hardware's approximate FP64 reciprocal,
+ * the IEEE division outside [2^-1000, 2^1000]): for each of the n host values
+ * compares it with the IEEE 1/x on the current device; *max_ulp is the largest
+ * distance in units in the last place, *mismatches the results that differ in
+ * class (finite / infinite / NaN) or sign. */
+int wpf_check_reciprocal(const double* host_values, int64_t n, int64_t* max_ulp, int64_t* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

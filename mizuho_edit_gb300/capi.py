@@ -118,6 +118,7 @@ SIGNATURES = {
     "wpf_ensemble_run": (C.c_int, [C.POINTER(H), C.c_int32, C.c_int32, C.c_int32, C.c_int32, DP,
                                    C.POINTER(StepStats), C.POINTER(C.c_int32)]),
     "wpf_check_conversions": (C.c_int, [DP, C.c_int64, C.POINTER(C.c_int64)]),
+    "wpf_check_reciprocal": (C.c_int, [DP, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     # include/wpf_net.h: the learned warm start
     "wpf_net_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "wpf_net_destroy": (C.c_int, [C.c_void_p]),

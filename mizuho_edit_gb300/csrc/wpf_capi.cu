@@ -817,7 +817,59 @@ __global__ void k_check_conversions(const double* x, long long n, unsigned long 
     }
     if (nb) atomicAdd(bad, nb);
 }
+
+// rcp_nr(x) against the IEEE 1/x: the largest distance in units in the last
+// place over the finite results, and the count of results that differ in
+// class (finite / infinite / NaN) or sign.
+__global__ void k_check_reciprocal(const double* x, long long n, unsigned long long* worst,
+                                   unsigned long long* bad) {
+    unsigned long long w = 0, nb = 0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const double v = x[q];
+        const double ref = 1.0 / v, got = rcp_nr(v);
+        const long long br = __double_as_longlong(ref), bg = __double_as_longlong(got);
+        const bool fr = isfinite(ref), fg = isfinite(got);
+        if (fr != fg || (!fr && !(isnan(ref) && isnan(got)) && br != bg) || (fr && ((br ^ bg) < 0))) {
+            ++nb;
+        } else if (fr) {
+            const unsigned long long d = br > bg ? (unsigned long long)(br - bg) : (unsigned long long)(bg - br);
+            if (d > w) w = d;
+        }
+    }
+    if (nb) atomicAdd(bad, nb);
+    if (w) atomicMax(worst, w);
+}
 }  // namespace wpf
+
+extern "C" int wpf_check_reciprocal(const double* host_values, int64_t n, int64_t* max_ulp,
+                                    int64_t* mismatches) {
+    using namespace wpf;
+    if (!host_values || n < 0 || !max_ulp || !mismatches) return WPF_ERR_ARG;
+    *max_ulp = 0;
+    *mismatches = 0;
+    if (n == 0) return WPF_OK;
+    double* d = nullptr;
+    unsigned long long* acc = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * n) != cudaSuccess || cudaMalloc(&acc, 2 * sizeof(*acc)) != cudaSuccess) {
+        cudaGetLastError();
+        if (d) cudaFree(d);
+        return WPF_ERR_NOMEM;
+    }
+    unsigned long long h[2] = {0, 0};
+    int rc = WPF_OK;
+    if (cudaMemcpy(d, host_values, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(acc, 0, 2 * sizeof(*acc)) != cudaSuccess)
+        rc = WPF_ERR_CUDA;
+    if (!rc) {
+        k_check_reciprocal<<<256, 256>>>(d, n, acc, acc + 1);
+        if (cudaMemcpy(h, acc, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) rc = WPF_ERR_CUDA;
+    }
+    cudaFree(d);
+    cudaFree(acc);
+    *max_ulp = (int64_t)h[0];
+    *mismatches = (int64_t)h[1];
+    return rc;
+}
 
 extern "C" int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatches) {
     using namespace wpf;

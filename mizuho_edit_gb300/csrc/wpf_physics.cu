@@ -321,7 +321,7 @@ __global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
     auto face = [&](long long m, bool inside, double* __restrict__ T, double* __restrict__ Kf,
                     double* __restrict__ Tv) {
         const double b = K0(m);
-        const double kf = a2 * b / (a + b);
+        const double kf = (a2 * b) * rcp_nr(a + b);
         const double t = inside ? kf * inv_mu : 0.0;
         if (rk) own += resid_face_delta(rk, fl, pr, n, m, p_a, t - T[n]);
         T[n] = t;

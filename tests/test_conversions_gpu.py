@@ -2,7 +2,9 @@
 agree with the hardware conversions: round to nearest even into FP32 over
 the whole FP32 normal range (ties, carries into the exponent, the overflow
 boundary), Inf and NaN, and exact FP32 -> FP64; arguments below 2^-126 flush
-to zero by design."""
+to zero by design.  The Newton-Raphson reciprocal of the harmonic means stays
+within two units in the last place of the IEEE 1/x, with the same class and
+sign of result, over the whole FP64 range."""
 import ctypes as C
 
 import numpy as np
@@ -40,3 +42,27 @@ def test_integer_pipe_conversions_match_hardware():
     capi.check(L.wpf_check_conversions(v.ctypes.data_as(capi.DP), v.size, C.byref(bad)),
                "wpf_check_conversions")
     assert bad.value == 0
+
+
+def test_newton_reciprocal_within_two_ulp():
+    from mizuho_edit_gb300 import capi
+    L = capi.load()
+    rng = np.random.default_rng(11)
+    e = rng.uniform(-1070.0, 1020.0, 400000)
+    parts = [
+        rng.choice([-1.0, 1.0], e.size) * rng.uniform(1.0, 2.0, e.size) * 2.0 ** np.floor(e),
+        rng.uniform(1e-13, 1e-9, 100000),            # permeability sums of the harmonic means
+        rng.uniform(1.0, 2.0, 100000),
+        # both sides of the guard exponents 2^-1000 and 2^1000, and the specials
+        np.ldexp(rng.uniform(1.0, 2.0, 2000), rng.integers(-1003, -997, 2000)),
+        np.ldexp(rng.uniform(1.0, 2.0, 2000), rng.integers(997, 1003, 2000)),
+        np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+                  np.finfo(np.float64).max, -np.finfo(np.float64).max, 1.0, -1.0, 0.5, 3.0]),
+    ]
+    v = np.ascontiguousarray(np.concatenate(parts), dtype=np.float64)
+    ulp = C.c_int64(-1)
+    bad = C.c_int64(-1)
+    capi.check(L.wpf_check_reciprocal(v.ctypes.data_as(capi.DP), v.size, C.byref(ulp), C.byref(bad)),
+               "wpf_check_reciprocal")
+    assert bad.value == 0
+    assert 0 <= ulp.value <= 2
