@@ -195,28 +195,34 @@ int wpf_run(wpf_handle* h, int32_t itime0, int32_t nsteps, double* dtime_inout,
 int wpf_reduce(wpf_handle* h, wpf_diag* d);
 
 /* Allocation-free diagnostics.  No counterpart in the reference: an addition
- * for callers that cannot call cudaMalloc -- code running while a CUDA graph
- * is captured (allocation cannot be captured), code whose device memory
- * belongs to another runtime's pool allocator, and latency-critical code that
- * cannot afford cudaMalloc's implicit device synchronisation.  It computes
- * pv, vcal, rwhmax and the phase / concentration max and min of wpf_diag
- * (pressure_ref and inlet_flux are returned as 0) from device arrays the
- * caller already holds: d_phase and d_concent are G-sized float64 arrays in
- * the reference layout (Fortran order with the one-cell halo).  Its scratch
- * is one fixed file-scope device array of WPF_NOALLOC_MAX_PLANES records
- * (about 360 KB), reserved on every GPU that loads the library until the
- * process exits; grids with nz + 2 > WPF_NOALLOC_MAX_PLANES are rejected with
- * WPF_ERR_TOO_LARGE.  The first call on a device looks up the scratch's
- * device address (once per device), so make that first call before any
- * stream capture.  Work is ordered on `stream` (a cudaStream_t; NULL = the
- * default stream) and the call returns after it finishes.  Every call shares
- * the one scratch array, so calls that overlap on the GPU race.             */
+ * for callers that cannot call cudaMalloc -- code whose device memory belongs
+ * to another runtime's pool allocator (which must account for every byte the
+ * process takes), and latency-critical code that cannot afford cudaMalloc's
+ * implicit device synchronisation.  It computes pv, vcal, rwhmax and the
+ * phase / concentration max and min of wpf_diag (pressure_ref and inlet_flux
+ * are returned as 0, phase_max_outlet as NaN) from device arrays the caller
+ * already holds: d_phase and d_concent are G-sized float64 arrays in the
+ * reference layout (Fortran order with the one-cell halo).  Its scratch is one
+ * fixed file-scope device array of WPF_NOALLOC_MAX_PLANES records (about
+ * 360 KB), reserved on every GPU that loads the library until the process
+ * exits; grids with nz + 2 > WPF_NOALLOC_MAX_PLANES are rejected with
+ * WPF_ERR_TOO_LARGE.  The first call on a device (and the first after a
+ * device reset) looks up the scratch's device address.  Work is ordered on
+ * `stream` (a cudaStream_t; NULL = the default stream) and the call returns
+ * after it finishes.  Every call shares the one scratch array, so calls that
+ * overlap on the GPU race.                                                  */
 #define WPF_NOALLOC_MAX_PLANES 4096
 int wpf_reduce_noalloc(const wpf_params* p, const double* d_phase, const double* d_concent,
                        wpf_diag* out, void* stream);
 
 /* Last taumin on the device (the lagged input of the dt law).               */
 int wpf_get_taumin(const wpf_handle* h, double* taumin);
+/* Set that lagged taumin, for a run that resumes at itime >= 3 from a saved
+ * state: the first resumed wpf_step then takes the step size the continuous
+ * run would have taken (wPFAW3D.f90:2227-2230).  The reference restarts from
+ * loadField (:509-557) at itime 0 and takes the configured dt for two steps;
+ * this is an addition.  taumin must be positive and finite.               */
+int wpf_set_taumin(wpf_handle* h, double taumin);
 
 /* The handle's CUDA stream (cudaStream_t), for callers that order their own
  * work or timing events with the library's; and the number of kernels the

@@ -652,6 +652,18 @@ int wpf_get_taumin(const wpf_handle* h, double* taumin) {
     return WPF_OK;
 }
 
+int wpf_set_taumin(wpf_handle* h, double taumin) {
+    if (!h || !(taumin > 0.0) || !(taumin < INFINITY)) return WPF_ERR_ARG;
+    h->taumin_last = taumin;   // the host-driven step's dt law
+    // and the key the device-resident step's dt law reads (the last update's min)
+    const unsigned long long key = dkey_host(taumin);
+    memcpy(&h->hsc[S_TAUMIN_KEY], &key, 8);
+    WPF_CUDA(cudaMemcpyAsync(h->dsc + S_TAUMIN_KEY, h->hsc + S_TAUMIN_KEY, sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream));
+    WPF_CUDA(cudaStreamSynchronize(h->stream));
+    return WPF_OK;
+}
+
 int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* st) {
     if (!h || !dtime_inout || !h->have_wells) return WPF_ERR_ARG;
     double dt = *dtime_inout;

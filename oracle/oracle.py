@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "libwpf_oracle.so")
 
 SOLVE_BCGS_SOR = 0
 SOLVE_CG = 1
+SOLVE_MGCG = 2   # same system and stopping test as SOLVE_CG; faster at 64^3 and up
 
 
 def build(force: bool = False) -> str:

@@ -477,6 +477,233 @@ static int solve_cg(const sysmat* A, double* x, double rtol, int maxit, orc_solv
 }
 
 /*
+ * Multigrid-preconditioned CG on the same SPD free-row system as solve_cg,
+ * stopped by the same test on the true residual ||b - A x|| <= rtol*||b||.
+ * Only the speed differs: at 128^3 Jacobi-PCG needs ~1300 iterations per
+ * solve, this ~15.  The converged pressure is a property of the assembled
+ * system (sys_build, wPFAW3D.f90:629-936), not of the solver.
+ *
+ * Preconditioner: one W-cycle over a hierarchy of 2x2x2 box aggregates
+ * (piecewise-constant interpolation P, coarse operator the Galerkin product
+ * P^T M P), symmetric red-black Gauss-Seidel (nu sweeps red->black before,
+ * black->red after), zero start on every level, exact solve on the final
+ * single cell; the whole cycle is a symmetric positive definite operator, as
+ * CG requires.  Cells with a zero diagonal (Dirichlet rows and aggregates of
+ * them) are inert.  The matrix is stored as a diagonal d > 0 and the six
+ * neighbour couplings c >= 0 (M x = d x - sum c x_nb).
+ */
+typedef struct {
+    int nx, ny, nz;
+    long N;
+    double *d, *ce, *cn, *ct;   /* couplings toward x+, y+, z+ (the x- coupling of cell q
+                                  is ce[q - 1], and so on: M is symmetric) */
+    double *x, *r, *t;
+} mg_level;
+
+#define MG_MAX_LEVELS 24
+#define MG_SERIAL_CELLS 32768   /* smaller levels run on one thread (fork/join costs more) */
+
+static double mg_row(const mg_level* L, long q, int i, int j, int k, const double* x) {
+    long sy = L->nx, sz = (long)L->nx * L->ny;
+    double s = 0.0;
+    if (i > 0) s += L->ce[q - 1] * x[q - 1];
+    if (i < L->nx - 1) s += L->ce[q] * x[q + 1];
+    if (j > 0) s += L->cn[q - sy] * x[q - sy];
+    if (j < L->ny - 1) s += L->cn[q] * x[q + sy];
+    if (k > 0) s += L->ct[q - sz] * x[q - sz];
+    if (k < L->nz - 1) s += L->ct[q] * x[q + sz];
+    return s;
+}
+
+/* One colour of a Gauss-Seidel sweep: x = (r + sum c x_nb) / d on the cells
+ * with (i + j + k) % 2 == colour. */
+static void mg_colour(mg_level* L, int colour) {
+#pragma omp parallel for schedule(static) if (L->N > MG_SERIAL_CELLS)
+    for (int k = 0; k < L->nz; ++k)
+        for (int j = 0; j < L->ny; ++j)
+            for (int i = (j + k + colour) & 1; i < L->nx; i += 2) {
+                long q = i + (long)L->nx * (j + (long)L->ny * k);
+                if (L->d[q] > 0.0) L->x[q] = (L->r[q] + mg_row(L, q, i, j, k, L->x)) / L->d[q];
+            }
+}
+
+/* t = r - M x */
+static void mg_resid(mg_level* L) {
+#pragma omp parallel for schedule(static) if (L->N > MG_SERIAL_CELLS)
+    for (int k = 0; k < L->nz; ++k)
+        for (int j = 0; j < L->ny; ++j)
+            for (int i = 0; i < L->nx; ++i) {
+                long q = i + (long)L->nx * (j + (long)L->ny * k);
+                L->t[q] = L->d[q] > 0.0 ? L->r[q] - (L->d[q] * L->x[q] - mg_row(L, q, i, j, k, L->x))
+                                        : 0.0;
+            }
+}
+
+static long mg_parent(const mg_level* F, const mg_level* Cl, long q) {
+    long i = q % F->nx, j = (q / F->nx) % F->ny, k = q / ((long)F->nx * F->ny);
+    return (i >> 1) + (long)Cl->nx * ((j >> 1) + (long)Cl->ny * (k >> 1));
+}
+
+static void mg_alloc(mg_level* L, int nx, int ny, int nz) {
+    L->nx = nx; L->ny = ny; L->nz = nz;
+    L->N = (long)nx * ny * nz;
+    double** a[7] = {&L->d, &L->ce, &L->cn, &L->ct, &L->x, &L->r, &L->t};
+    for (int m = 0; m < 7; ++m) *a[m] = (double*)calloc((size_t)L->N, sizeof(double));
+}
+
+static void mg_free(mg_level* L) {
+    free(L->d); free(L->ce); free(L->cn); free(L->ct);
+    free(L->x); free(L->r); free(L->t);
+}
+
+/* Galerkin coarse operator of 2x2x2 aggregation: the diagonal of aggregate I
+ * is sum_{i,j in I} M_ij, its coupling toward the next aggregate along an
+ * axis is the sum of the fine couplings across the shared face.  Gathered
+ * per coarse cell (the fine cells of one aggregate are its children). */
+static void mg_coarsen(const mg_level* F, mg_level* Cl) {
+    mg_alloc(Cl, (F->nx + 1) / 2, (F->ny + 1) / 2, (F->nz + 1) / 2);
+#pragma omp parallel for schedule(static) if (F->N > MG_SERIAL_CELLS)
+    for (int K = 0; K < Cl->nz; ++K)
+        for (int J = 0; J < Cl->ny; ++J)
+            for (int I = 0; I < Cl->nx; ++I) {
+                long P = I + (long)Cl->nx * (J + (long)Cl->ny * K);
+                double d = 0.0, ce = 0.0, cn = 0.0, ct = 0.0;
+                for (int k = 2 * K; k < 2 * K + 2 && k < F->nz; ++k)
+                    for (int j = 2 * J; j < 2 * J + 2 && j < F->ny; ++j)
+                        for (int i = 2 * I; i < 2 * I + 2 && i < F->nx; ++i) {
+                            long q = i + (long)F->nx * (j + (long)F->ny * k);
+                            if (!(F->d[q] > 0.0)) continue;
+                            d += F->d[q];
+                            /* a face inside the aggregate counts twice against the
+                               diagonal (once from each side); a face toward a dead
+                               neighbour carries no coupling (c = 0) */
+                            if (i + 1 < F->nx) {
+                                if (i == 2 * I + 1) ce += F->ce[q]; else d -= 2.0 * F->ce[q];
+                            }
+                            if (j + 1 < F->ny) {
+                                if (j == 2 * J + 1) cn += F->cn[q]; else d -= 2.0 * F->cn[q];
+                            }
+                            if (k + 1 < F->nz) {
+                                if (k == 2 * K + 1) ct += F->ct[q]; else d -= 2.0 * F->ct[q];
+                            }
+                        }
+                Cl->d[P] = d > 1e-300 ? d : 0.0;
+                Cl->ce[P] = I < Cl->nx - 1 ? ce : 0.0;
+                Cl->cn[P] = J < Cl->ny - 1 ? cn : 0.0;
+                Cl->ct[P] = K < Cl->nz - 1 ? ct : 0.0;
+            }
+}
+
+/* Cl->r = P^T t (sum of the live children's residuals). */
+static void mg_restrict(const mg_level* F, mg_level* Cl) {
+#pragma omp parallel for schedule(static) if (F->N > MG_SERIAL_CELLS)
+    for (int K = 0; K < Cl->nz; ++K)
+        for (int J = 0; J < Cl->ny; ++J)
+            for (int I = 0; I < Cl->nx; ++I) {
+                double s = 0.0;
+                for (int k = 2 * K; k < 2 * K + 2 && k < F->nz; ++k)
+                    for (int j = 2 * J; j < 2 * J + 2 && j < F->ny; ++j)
+                        for (int i = 2 * I; i < 2 * I + 2 && i < F->nx; ++i) {
+                            long q = i + (long)F->nx * (j + (long)F->ny * k);
+                            if (F->d[q] > 0.0) s += F->t[q];
+                        }
+                Cl->r[I + (long)Cl->nx * (J + (long)Cl->ny * K)] = s;
+            }
+}
+
+/* One W-cycle for M_l x = r_l from the current x of level l: the coarse
+ * problem is visited twice (its second visit continues from the first). */
+static void mg_cycle(mg_level* lv, int nlev, int l, int nu) {
+    mg_level* L = &lv[l];
+    if (l == nlev - 1) {                      /* the single-cell level: exact */
+        for (int s = 0; s < 2; ++s) { mg_colour(L, 0); mg_colour(L, 1); mg_colour(L, 1); mg_colour(L, 0); }
+        return;
+    }
+    mg_level* Cl = &lv[l + 1];
+    for (int s = 0; s < nu; ++s) { mg_colour(L, 0); mg_colour(L, 1); }
+    mg_resid(L);
+    mg_restrict(L, Cl);
+    memset(Cl->x, 0, (size_t)Cl->N * sizeof(double));
+    mg_cycle(lv, nlev, l + 1, nu);
+    if (l + 1 < nlev - 1) mg_cycle(lv, nlev, l + 1, nu);
+#pragma omp parallel for schedule(static) if (L->N > MG_SERIAL_CELLS)
+    for (long q = 0; q < L->N; ++q) if (L->d[q] > 0.0) L->x[q] += Cl->x[mg_parent(L, Cl, q)];
+    for (int s = 0; s < nu; ++s) { mg_colour(L, 1); mg_colour(L, 0); }
+}
+
+static int solve_mgcg(const sysmat* A, double* x, double rtol, int maxit, orc_solve_info* info) {
+    long N = A->N;
+    mg_level lv[MG_MAX_LEVELS];
+    int nlev = 1;
+    mg_alloc(&lv[0], A->nx, A->ny, A->nz);
+    for (long q = 0; q < N; ++q) {
+        if (A->dir[q]) continue;
+        lv[0].d[q] = -A->cC[q];
+        lv[0].ce[q] = A->cE[q]; lv[0].cn[q] = A->cN[q]; lv[0].ct[q] = A->cT[q];
+    }
+    while (nlev < MG_MAX_LEVELS && lv[nlev - 1].N > 1) {
+        mg_coarsen(&lv[nlev - 1], &lv[nlev]);
+        ++nlev;
+    }
+    double *r = malloc(N * sizeof(double)), *pv = malloc(N * sizeof(double)),
+           *q = malloc(N * sizeof(double));
+    double* z = lv[0].x;
+    double bnorm = sqrt(dot(A->b, A->b, N));
+    for (long n = 0; n < N; ++n) if (A->dir[n]) x[n] = A->b[n];
+    double tol = rtol * bnorm;
+    int it = 0, conv = 0;
+    double rnorm = 0.0;
+    for (int restart = 0; restart < 50 && !conv; ++restart) {
+        sys_mult(A, x, q);
+#pragma omp parallel for schedule(static)
+        for (long n = 0; n < N; ++n) r[n] = A->dir[n] ? 0.0 : (A->b[n] - q[n]);
+        rnorm = sqrt(dot(r, r, N));
+        if (rnorm <= tol) { conv = 1; break; }
+        if (!(rnorm == rnorm) || isinf(rnorm)) break;
+        if (it >= maxit) break;
+        /* M = -A on free rows: x solves M x = -b, whose residual is -r_A. */
+        for (long n = 0; n < N; ++n) r[n] = -r[n];
+        memcpy(lv[0].r, r, N * sizeof(double));
+        memset(z, 0, N * sizeof(double));
+        mg_cycle(lv, nlev, 0, 1);
+        memcpy(pv, z, N * sizeof(double));
+        double rz = dot(r, z, N);
+        int inner = 0;
+        while (it < maxit && inner < 200) {
+            sys_mult(A, pv, q);
+#pragma omp parallel for schedule(static)
+            for (long n = 0; n < N; ++n) q[n] = A->dir[n] ? 0.0 : -q[n];
+            double pq = dot(pv, q, N);
+            if (pq == 0.0) break;
+            double al = rz / pq;
+#pragma omp parallel for schedule(static)
+            for (long n = 0; n < N; ++n) {
+                x[n] += al * pv[n];
+                r[n] -= al * q[n];
+            }
+            ++it; ++inner;
+            double rr = sqrt(dot(r, r, N));
+            if (rr <= 0.5 * tol || !(rr == rr) || isinf(rr)) break;
+            memcpy(lv[0].r, r, N * sizeof(double));
+            memset(z, 0, N * sizeof(double));
+            mg_cycle(lv, nlev, 0, 1);
+            double rz2 = dot(r, z, N);
+            double be = rz2 / rz;
+            rz = rz2;
+#pragma omp parallel for schedule(static)
+            for (long n = 0; n < N; ++n) pv[n] = z[n] + be * pv[n];
+        }
+    }
+    info->iterations = it;
+    info->converged = conv;
+    info->rnorm = rnorm;
+    info->bnorm = bnorm;
+    free(r); free(pv); free(q);
+    for (int l = 0; l < nlev; ++l) mg_free(&lv[l]);
+    return conv ? 0 : 1;
+}
+
+/*
  * solvePressure, wPFAW3D.f90:603-1160: build the system (:629-936), solve it
  * warm-started from the current pressure (:977-986), copy the result into
  * the interior (:1048) and refresh the halo (:1050).
@@ -496,6 +723,7 @@ int orc_solve_pressure(orc_state* s, int mode, double rtol, int maxit, int nbloc
     if (!info) info = &tmp;
     memset(info, 0, sizeof(*info));
     int rc = mode == ORC_SOLVE_BCGS_SOR ? solve_bcgs(&A, x, rtol, maxit, nblocks, info)
+             : mode == ORC_SOLVE_MGCG   ? solve_mgcg(&A, x, rtol, maxit, info)
                                         : solve_cg(&A, x, rtol, maxit, info);
     /* true relative residual of the returned iterate */
     double* y = malloc(N * sizeof(double));

@@ -70,6 +70,7 @@ typedef struct orc_state {
 /* Solver modes of orc_solve_pressure. */
 #define ORC_SOLVE_BCGS_SOR 0   /* mirror of KSPBCGS + PCSOR(10,1,1.7), wPFAW3D.f90:988-1004 */
 #define ORC_SOLVE_CG       1   /* Jacobi-PCG on the SPD free-cell system, tight true residual */
+#define ORC_SOLVE_MGCG     2   /* the same system and stopping test, multigrid-preconditioned CG */
 
 typedef struct orc_solve_info {
     int32_t iterations;

@@ -21,6 +21,8 @@ def _driver():
 
 
 def _write_case(tmp_path, n=(16, 12, 10), seed=5):
+    import pathlib
+    tmp_path = pathlib.Path(tmp_path)
     case = make_case(n, seed=seed, log_var=1.0, corr_len=3.0)
     p = case.params
     p.time_total = 1000.0                  # --nsteps ends the run
@@ -109,4 +111,51 @@ def test_driver_runs_a_case(tmp_path):
     # the last .res block holds the final fields in single precision
     perm = [r for r in res if r[0] == "Phase-field"][-1][2]["v"]
     assert np.allclose(perm, f["phase"][1:-1, 1:-1, 1:-1].ravel(order="F").astype(np.float32))
-    assert os.path.getsize(str(tmp_path / "case.last.fld.p")) == 8 * 18 * 14 * 12
+    # the pressure side file: the halo pressure, then a 32-byte step trailer
+    assert os.path.getsize(str(tmp_path / "case.last.fld.p")) == 8 * 18 * 14 * 12 + 32
+
+
+@pytest.mark.gpu
+def test_restart_resumes_the_run(tmp_path):
+    """N steps, the restart field and its pressure side file (saveField,
+    wPFAW3D.f90:2096-2141), a restart from them (loadField, :509-557) and M
+    more steps give the fields of N + M continuous steps: same step count,
+    time and step size, phase, concentration and pressure within 1e-12."""
+    from mizuho_edit_gb300.fld import read_fld
+    n, steps_a, steps_b = (16, 12, 10), 9, 7
+    G = (n[0] + 2) * (n[1] + 2) * (n[2] + 2)
+
+    def run(cfg, nsteps):
+        r = subprocess.run([_driver(), cfg, "--nsteps", str(nsteps), "--rtol", "1e-13", "--quiet"],
+                           capture_output=True, text=True, cwd=os.path.dirname(cfg))
+        assert r.returncode == 0, r.stderr
+
+    def side(path):
+        raw = open(path, "rb").read()
+        assert len(raw) == 8 * G + 32 and raw[8 * G:8 * G + 8] == b"WPFSTEP1"
+        pr = np.frombuffer(raw[:8 * G], np.float64)
+        itime, dt, taumin = np.frombuffer(raw[8 * G + 8:], np.float64)
+        return pr, int(itime), dt, taumin
+
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
+    _, cont = _write_case(tmp_path / "a", n)
+    run(cont, steps_a + steps_b)
+    _, first = _write_case(tmp_path / "b", n)
+    run(first, steps_a)
+    pr_a, it_a, _, _ = side(str(tmp_path / "b" / "case.last.fld.p"))
+    assert it_a == steps_a
+    p = config.load_config(first)
+    p.filename_last = "case2.last.fld"
+    config.write_config(str(tmp_path / "b" / "case2.cfg"), p, "wells.dat", "case.last.fld")
+    run(str(tmp_path / "b" / "case2.cfg"), steps_b)
+    want = read_fld(str(tmp_path / "a" / "case.last.fld"), expect_grid=n)
+    got = read_fld(str(tmp_path / "b" / "case2.last.fld"), expect_grid=n)
+    pw, itw, dtw, tmw = side(str(tmp_path / "a" / "case.last.fld.p"))
+    pg, itg, dtg, tmg = side(str(tmp_path / "b" / "case2.last.fld.p"))
+    assert itg == itw == steps_a + steps_b
+    assert dtg == pytest.approx(dtw, rel=1e-12) and tmg == pytest.approx(tmw, rel=1e-12)
+    assert got.time == pytest.approx(want.time, rel=1e-12)
+    assert rel_l2(got.phase, want.phase) < 1e-12
+    assert rel_l2(got.concent, want.concent) < 1e-12
+    assert rel_l2(pg, pw) < 1e-12

@@ -72,6 +72,35 @@ def test_solvers_match_direct(oracle_mod, seed, lv):
     info3 = s3.solvePressure(oracle_mod.SOLVE_BCGS_SOR, 1e-10, 1000, 4)
     assert info3.converged
     assert rel_l2(s3.pressure[1:-1, 1:-1, 1:-1].ravel(order="F"), x) < 1e-7
+    # the multigrid-preconditioned CG of the long parity runs: same system,
+    # same stopping test, same solution as the direct solve
+    s4 = _sim(oracle_mod, case)
+    s4.calcPermeability()
+    info4 = s4.solvePressure(oracle_mod.SOLVE_MGCG, 1e-14)
+    assert info4.converged and info4.true_relres <= 1e-14
+    assert info4.iterations < info.iterations
+    assert rel_l2(s4.pressure[1:-1, 1:-1, 1:-1].ravel(order="F"), x) < 1e-12
+
+
+@pytest.mark.parametrize("n", [(7, 5, 3), (17, 9, 6), (32, 32, 32)])
+def test_mgcg_matches_cg_with_injection(oracle_mod, n):
+    """Multigrid CG against Jacobi CG on odd and even grids, rough interface
+    state, an injection well (wpq = -1, wPFAW3D.f90:815-817) and the
+    Dirichlet outlet; aggregates that hold only Dirichlet cells are inert."""
+    from mizuho_edit_gb300.cases import grf
+    from mizuho_edit_gb300.config import Well
+    case = _case(n, seed=5, log_var=2.0, corr_len=3.0)
+    p = case.params
+    case.phase = np.tanh(1.5 * grf(n, 2.0, 9))
+    p.wells = [w for w in p.wells if w.ix == p.nx] + [
+        Well(1, 1 + n[1] // 2, 1 + n[2] // 2, pressure=0.0, injection=0.05, phase=1.0, concent=1.0)]
+    a, b = _sim(oracle_mod, case), _sim(oracle_mod, case)
+    a.calcPermeability()
+    b.calcPermeability()
+    ia = a.solvePressure(oracle_mod.SOLVE_MGCG, 1e-14)
+    ib = b.solvePressure(oracle_mod.SOLVE_CG, 1e-14)
+    assert ia.converged and ib.converged
+    assert rel_l2(a.pressure, b.pressure) < 1e-12
 
 
 def test_homogeneous_linear_pressure(oracle_mod):
