@@ -128,6 +128,9 @@ typedef struct wpf_step_stats {
     int32_t warm_start;        /* 1: the solve started from the extrapolated p + e;
                                   -1: it was tried and rejected; 0: not tried         */
     double relres0;            /* relative residual of the warm start                  */
+    int32_t active_cells;      /* cells the fused update evaluated in FP64 (interface and
+                                  concentration work lists; the rest were copies)       */
+    int32_t pad;
 } wpf_step_stats;
 
 /* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */

@@ -699,6 +699,7 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     s->dtime = dt;
     s->max_courant = umax * dt / p.dx;
     s->kernel_launches = (int32_t)(h->nlaunch - l0);
+    s->active_cells = (int32_t)h->last_active;
     *dtime_inout = dt;
     return srs;
 }

@@ -348,6 +348,7 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
         st->dtime = c.dt;
         st->max_courant = umax * c.dt / h->prm.dx;
         st->kernel_launches = (int32_t)launches;
+        st->active_cells = (int32_t)h->last_active;
     }
     cudaGetLastError();
     if (dt_out) *dt_out = c.dt;

@@ -122,9 +122,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Shared memory of a conv CTA: two stages; allocated with room to spare so
-// that every descriptor-addressed read stays inside the allocation.
-constexpr int CONV_SMEM = 96 * 1024;
+// Shared memory of a conv CTA: two stages of A (128 rows) and B (COUT rows),
+// plus 1 KB so that every descriptor-addressed read stays inside the
+// allocation.  Sized per shape: the 16-channel layers take 10 KB, so many
+// CTAs share an SM and hide each other's gather latency.
+constexpr int CONV_SMEM_MAX = 96 * 1024;
+template <int CIN, int COUT>
+constexpr int conv_smem() { return 2 * (CIN * 256 + COUT * CIN * 2) + 1024; }
+constexpr int WG_STAGE_ = 32;
+template <int CIN, int COUT>
+constexpr int wgrad_smem() { return 2 * (128 * WG_STAGE_ * 2 + COUT * WG_STAGE_ * 2) + 1024; }
 
 struct ConvArgs {
     int nx, ny, nz, nvox;
@@ -145,7 +152,8 @@ __global__ void __launch_bounds__(CT) k_conv3d(ConvArgs a) {
     constexpr int AB = CIN * 256;        // 128 rows x CIN bf16
     constexpr int BB = COUT * CIN * 2;   // COUT rows x CIN bf16
     constexpr int SB = AB + BB;
-    static_assert(2 * SB <= CONV_SMEM, "conv stages exceed the shared allocation");
+    static_assert(2 * SB + 1024 == conv_smem<CIN, COUT>() && conv_smem<CIN, COUT>() <= CONV_SMEM_MAX,
+                  "conv stages exceed the shared allocation");
     constexpr uint32_t NCOL = COUT < 32 ? 32 : COUT;
     constexpr uint32_t IDESC = idesc_bf16(128, COUT);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(CT) k_conv3d(ConvArgs a) {
 // CTA (blockIdx.x = 128-row tile of r, blockIdx.y = chunk of WG_VOX voxels);
 // stages of 32 voxels (two MMAs of K = 16), FP32 atomics into gw.
 constexpr int WG_VOX = 2048;
-constexpr int WG_STAGE = 32;
+constexpr int WG_STAGE = WG_STAGE_;
 
 struct WgradArgs {
     int nx, ny, nz, nvox;
@@ -263,7 +271,8 @@ __global__ void __launch_bounds__(CT) k_conv3d_wgrad(WgradArgs a) {
     constexpr int AB = 128 * WG_STAGE * 2;    // 128 rows x 32 voxels bf16
     constexpr int BB = COUT * WG_STAGE * 2;
     constexpr int SB = AB + BB;
-    static_assert(2 * SB <= CONV_SMEM, "wgrad stages exceed the shared allocation");
+    static_assert(2 * SB + 1024 == wgrad_smem<CIN, COUT>() && wgrad_smem<CIN, COUT>() <= CONV_SMEM_MAX,
+                  "wgrad stages exceed the shared allocation");
     constexpr uint32_t NCOL = COUT < 32 ? 32 : COUT;
     constexpr uint32_t IDESC = idesc_bf16(128, COUT);
     constexpr int R = 27 * CIN;
@@ -552,11 +561,11 @@ static int launch_conv_t(const ConvArgs& a, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         WPF_CUDA(cudaFuncSetAttribute(k_conv3d<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      CONV_SMEM));
+                                      conv_smem<CIN, COUT>()));
         attr = true;
     }
     const unsigned grid = (unsigned)((a.nvox + CT - 1) / CT);
-    k_conv3d<CIN, COUT><<<grid, CT, CONV_SMEM, s>>>(a);
+    k_conv3d<CIN, COUT><<<grid, CT, conv_smem<CIN, COUT>(), s>>>(a);
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
@@ -575,11 +584,11 @@ static int launch_wgrad_t(const WgradArgs& a, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         WPF_CUDA(cudaFuncSetAttribute(k_conv3d_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      CONV_SMEM));
+                                      wgrad_smem<CIN, COUT>()));
         attr = true;
     }
     const dim3 grid((27 * CIN + CT - 1) / CT, (unsigned)((a.nvox + WG_VOX - 1) / WG_VOX));
-    k_conv3d_wgrad<CIN, COUT><<<grid, CT, CONV_SMEM, s>>>(a);
+    k_conv3d_wgrad<CIN, COUT><<<grid, CT, wgrad_smem<CIN, COUT>(), s>>>(a);
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
