@@ -2,11 +2,18 @@
 """Time-steps/s of the wPFAW3D time step on GB300.
 
 Workload: one 256^3 synthetic wormholing domain (K = exp(sigma g), log-K
-variance 2, correlation length 8 cells, seeded), Darcy solve to a 1e-8
-relative residual with the FP32 MG-PCG inside FP64 iterative refinement,
-then the fused phase / concentration update.  A "step" is one pass of the
-main-loop body (wPFAW3D.f90:2226-2280).  Inputs (all FP64 fields, ~2 GB)
-are far larger than the 129 MB L2, so no flush is needed between steps.
+variance 2, correlation length 8 cells, seeded; dissolved-rock permeability
+kwh = 1e3 x the geometric-mean rock K), Darcy solve to a 1e-8 relative
+residual.  A "step" is one pass of the main-loop body (wPFAW3D.f90:2226-2280).
+
+One run is advanced with the FP32-refined, extrapolated form; at each window
+(by default after 40 and after 2000 steps) every arm is timed on the run's
+state: the learned start (the headline, `value`), the extrapolated start
+without the network, and the plain FP64 MG-PCG from the previous pressure.
+The headline is the last window, where the acid has reached almost every
+cell and the fused update works on the whole grid.  A second run at kwh = 20
+is reported beside it.  Inputs (FP64 fields and solver levels, ~3.5 GB) are
+far larger than the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -31,9 +38,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-METRIC = "time-steps/s at 256^3, 1e-8 Darcy residual: warm-started FP32-refined vs plain FP64"
+METRIC = "time-steps/s at 256^3, 1e-8 Darcy residual: learned+FP32-refined vs plain FP64"
 KC_NAMES = ["permeability", "resid64", "coefficients", "smooth_l0", "mg_other", "apply",
             "pcg_vec", "fused_update", "other", "bottom"]
+# the timed forms ("arms") of the Darcy solve, all on the same run's state
+ARMS = ("learned", "extrapolated", "plain_fp64")
 
 
 def parse():
@@ -43,55 +52,55 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="cells per axis")
-    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--log-var", type=float, default=2.0)
     ap.add_argument("--corr", type=float, default=8.0)
+    ap.add_argument("--kwh", type=float, default=1000.0,
+                    help="permeability of dissolved rock (1e3 x the geometric-mean rock K)")
+    ap.add_argument("--kwh-alt", type=float, default=20.0,
+                    help="a second run at this kwh, reported beside the headline (0: none)")
     ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--windows", default="40,2000",
+                    help="steps run before each timed window; the headline is the last window")
+    ap.add_argument("--headline", default="learned", choices=["learned", "extrapolated"],
+                    help="the FP32-refined form whose time-steps/s is `value`")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned arm (the headline becomes the extrapolated form)")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--w-from", type=int, default=3,
-                    help="first multigrid level cycled twice (0 = library default, 2); 3 is the "
-                         "fastest at 256^3 of 2, 3, 4 and a V-cycle (same PCG iterations as 2)")
-    ap.add_argument("--breakdown", action="store_true",
-                    help="time every kernel class (diagnostic run; adds event overhead)")
+                    help="first multigrid level cycled twice in the FP32-refined forms (3: the "
+                         "fastest at 256^3 of 2, 3, 4 and a V-cycle)")
     ap.add_argument("--plain-w-from", type=int, default=2,
-                    help="W-cycle level of the plain FP64 comparison run (2: its fewest PCG "
-                         "iterations; from level 3 it takes 7 instead of 5 at 256^3)")
+                    help="W-cycle level of the plain FP64 arm (2: its fewest PCG iterations)")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="time every kernel class in an extra host-driven window (diagnostic)")
     ap.add_argument("--nu", type=int, default=2, help="smoothing sweeps per side of a cycle")
     ap.add_argument("--sweep-min", type=int, default=0,
                     help="cells from which a level uses the pipelined sweep (0 = library default)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the preconditioner cycle kernel by kernel")
-    ap.add_argument("--no-plain", action="store_true",
-                    help="skip the plain FP64 MG-PCG comparison run")
     ap.add_argument("--no-tma", action="store_true",
                     help="stage the finest-level sweep with cp.async instead of bulk-tensor copies")
-    ap.add_argument("--no-learned", action="store_true",
-                    help="skip the run with the learned correction of the start")
-    ap.add_argument("--spinup", type=int, default=40,
-                    help="untimed steps before the warm-up: the timed window starts past "
-                         "the start-up transient of the run (dt jump at step 3, first front "
-                         "motion), as in the 500-2000-step runs the metric stands for")
     ap.add_argument("--no-step-graph", action="store_true",
-                    help="host-driven steps (a read-back per PCG iteration) instead of one "
-                         "graph launch per step with the solver loops on the device")
-    ap.add_argument("--warm-start", default="extrap", choices=["none", "extrap"],
-                    help="start of each solve: previous pressure, or extrapolated in time")
+                    help="host-driven steps instead of one graph launch per step")
     return ap.parse_args()
 
 
-def solver_kwargs(args, solver=None):
-    """Solver options of the timed arm; solver="fp64" gives the plain method
-    (FP64 MG-PCG started from the previous pressure, as the reference)."""
-    plain = solver == "fp64"
-    return dict(solver=solver or args.solver, rtol=args.rtol,
+def arm_kwargs(args, arm):
+    """Solver options of an arm.  plain_fp64: the plain method, FP64 MG-PCG
+    from the previous pressure (the reference's start, wPFAW3D.f90:980);
+    extrapolated: FP32 MG-PCG inside FP64 refinement from the pressure
+    extrapolated in time; learned: the same plus the network's correction of
+    the extrapolation.  All finish at the same FP64 relative residual."""
+    plain = arm == "plain_fp64"
+    return dict(mode="fp64" if plain else "mixed", rtol=args.rtol,
                 w_from_level=args.plain_w_from if plain else args.w_from,
                 smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min,
                 graphs=not args.no_graphs, tma=not args.no_tma,
-                step_graph=not args.no_step_graph,
-                extrapolate=(not plain) and args.warm_start == "extrap")
+                step_graph=not args.no_step_graph, extrapolate=not plain)
 
 
 def dist_env():
@@ -187,29 +196,47 @@ def sweep_traffic_per_cell():
     return None
 
 
-def make_workload(args, rank):
+def make_workload(args, rank, kwh=None):
     from mizuho_edit_gb300.cases import make_case
     n = args.n
-    return make_case((n, n, n), log_var=args.log_var, corr_len=args.corr, seed=args.seed + rank)
+    return make_case((n, n, n), log_var=args.log_var, corr_len=args.corr, seed=args.seed + rank,
+                     kwh=args.kwh if kwh is None else kwh)
+
+
+def windows_of(args):
+    return [int(w) for w in args.windows.split(",") if w.strip()]
+
+
+def headline_arm(args):
+    return "extrapolated" if args.no_learned else args.headline
+
+
+def workload_name(args, kwh=None):
+    n = args.n
+    return (f"wPFAW3D step, {n}^3 cells, synthetic GRF log-K var {args.log_var} corr {args.corr}, "
+            f"kwh {args.kwh if kwh is None else kwh}, Pe 100, Da 10, Dirichlet p 1->0")
 
 
 def config_of(args, world):
     n = args.n
-    return {"workload": f"wPFAW3D step, {n}^3 cells, synthetic GRF log-K var {args.log_var} "
-                        f"corr {args.corr}, Pe 100, Da 10, Dirichlet p 1->0",
-            "grid": [n, n, n], "solver": "fp32-mg-pcg-in-fp64-refinement" if args.solver == "mixed"
-            else "fp64-mg-pcg", "darcy_rtol": args.rtol, "dtype_state": "f64",
-            "warm_start": ("time-extrapolated pressure with fallback to the previous pressure"
-                           if args.warm_start == "extrap" and args.solver == "mixed"
-                           else "previous pressure"),
-            "compared_with": f"plain FP64 MG-PCG from the previous pressure (plain_fp64; W-cycle "
-                             f"from level {args.plain_w_from})",
-            "timed_steps": f"{args.spinup + args.warmup + 1}..{args.spinup + args.warmup + args.steps}"
-                           f" of the run (spin-up {args.spinup} + warm-up {args.warmup} untimed)",
+    w = windows_of(args)
+    arm = headline_arm(args)
+    start = {"learned": "time-extrapolated pressure plus the learned network's correction "
+                        "(fallback to the previous pressure when it does not lower the FP64 residual)",
+             "extrapolated": "time-extrapolated pressure (fallback to the previous pressure)"}[arm]
+    return {"workload": workload_name(args), "grid": [n, n, n],
+            "solver": "fp32-mg-pcg-in-fp64-refinement", "darcy_rtol": args.rtol, "dtype_state": "f64",
+            "warm_start": start, "form": arm,
+            "compared_with": f"plain FP64 MG-PCG from the previous pressure on the same state "
+                             f"(plain_fp64; W-cycle from level {args.plain_w_from})",
+            "timed_steps": f"{w[-1] + args.warmup + 1}..{w[-1] + args.warmup + args.steps} of the run "
+                           f"(spin-up {w[-1]} steps + warm-up {args.warmup} untimed)",
+            "spinup_form": "extrapolated FP32-refined start, one graph launch per step",
             "multigrid": {"w_cycle_from_level": args.w_from, "sweeps_per_side": args.nu,
                           "pipelined_sweep_min_cells": args.sweep_min or (1 << 23)},
-            "step": "one CUDA graph launch per step" if not args.no_step_graph else "host-driven",
-            "l2_policy": "inputs larger than L2 (~2 GB of fields per step)",
+            "step": ("one CUDA graph launch per step" if not args.no_step_graph else "host-driven")
+                    + ("; the learned arm is host-driven" if arm == "learned" else ""),
+            "l2_policy": "inputs larger than L2 (~3.5 GB of fields and solver levels per step)",
             "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
 
 
@@ -236,81 +263,130 @@ def cpu_sample(sim, args):
                       f"{threads} OpenMP threads as {threads} SOR blocks), {dt:.1f} s"}
 
 
-def run_ours(args):
-    import torch
+class Arms:
+    """One simulation whose Darcy-solve form can be switched between the
+    arms; every arm is timed on the same state of the same run."""
+
+    def __init__(self, args, case, want_net):
+        from mizuho_edit_gb300.sim import Simulation
+        self.args = args
+        kw = arm_kwargs(args, "extrapolated")
+        self.sim = Simulation(case.params, case.permeab_rock, case.phase, case.concent,
+                              solver=kw.pop("mode"), **kw)
+        self.net = None
+        self.arm = "extrapolated"
+        if want_net:
+            from mizuho_edit_gb300 import learned
+            if os.path.exists(learned.DEFAULT_WEIGHTS):
+                n = args.n
+                self.net = learned.WarmStartNet(n // 2, n // 2, n // 2)
+                self.net.set_params(learned.WarmStartNet.load_params(learned.DEFAULT_WEIGHTS))
+
+    def set(self, arm):
+        from mizuho_edit_gb300 import learned
+        if arm == self.arm:
+            return
+        self.sim.set_solver(**arm_kwargs(self.args, arm))
+        learned.attach(self.sim, self.net if arm == "learned" else None)
+        self.arm = arm
+
+    def stream(self):
+        import torch
+        from mizuho_edit_gb300 import capi
+        sp = C.c_void_p()
+        capi.check(self.sim.L.wpf_get_stream(self.sim.h, C.byref(sp)), "wpf_get_stream")
+        return torch.cuda.ExternalStream(sp.value)
+
+    def advance_to(self, step):
+        self.set("extrapolated")
+        while self.sim.itime < step:
+            self.sim.step()
+
+    def time(self, arm, world, clocks=None):
+        """(clocks: a running ClockSampler, stopped after the timed steps.)"""
+        """W warm-up steps of the arm, then exactly K timed steps between a
+        barrier + synchronize and a synchronize, CUDA events on the library's
+        stream; max over ranks."""
+        import torch
+        args, sim = self.args, self.sim
+        self.set(arm)
+        for _ in range(args.warmup):
+            sim.step()
+        stream = self.stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0, n1 = C.c_int64(), C.c_int64()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        sim.L.wpf_launch_count(sim.h, C.byref(n0))
+        first = sim.itime + 1
+        e0.record(stream)
+        stats = [sim.step() for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sim.L.wpf_launch_count(sim.h, C.byref(n1))
+        clk = clocks.stop() if clocks else None
+        ms = max_over_ranks(e0.elapsed_time(e1), world)
+        ncell = args.n ** 3
+        out = {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
+               "window": [first, first + args.steps - 1], "ms_per_step": ms / args.steps,
+               "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
+               "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
+               "outer_passes_per_step": statistics.mean(s.outer_iterations for s in stats),
+               "relres0_mean": statistics.mean(s.relres0 for s in stats),
+               "relres_max": max(s.relres for s in stats),
+               "fused_update_ms": statistics.mean(s.update_ms for s in stats),
+               "update_active_fraction": statistics.mean(s.active_cells for s in stats) / ncell,
+               "max_courant": max(s.max_courant for s in stats),
+               "gpu_launches": int(n1.value - n0.value)}
+        if arm != "plain_fp64":
+            codes = [s.warm_start for s in stats]
+            out["starts"] = {"net": codes.count(2), "extrapolation": codes.count(1),
+                             "previous_pressure": codes.count(-1)}
+        if clk is not None:
+            out["clocks"] = clk
+        return out
+
+    def close(self):
+        from mizuho_edit_gb300 import learned
+        if self.sim is not None:
+            learned.attach(self.sim, None)
+            self.sim.close()
+            self.sim = None
+        if self.net is not None:
+            self.net.close()
+            self.net = None
+
+
+def roofline_window(args, arms):
+    """The finest-level red-black sweep timed per launch (the step's largest
+    HBM-bound share): its kernel class is timed with events around every
+    launch, which makes the steps host-driven, so this is a separate window
+    right after the timed ones (extrapolated arm)."""
     from mizuho_edit_gb300 import capi
-    from mizuho_edit_gb300.sim import Simulation
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    else:
-        torch.cuda.set_device(0)
-    dev = torch.cuda.current_device()
-    case = make_workload(args, rank)
-    sim = Simulation(case.params, case.permeab_rock, case.phase, case.concent,
-                     **solver_kwargs(args))
+    sim = arms.sim
     L = sim.L
     KC_SMOOTH0 = 3
     NK = len(KC_NAMES)
-    # Kernel-class timers bracket every launch with events, and a step with
-    # timers on is host-driven (the device-resident step graph is off while
-    # they are): the timed steps run without them, except in a --breakdown run;
-    # the per-launch time of the roofline kernel comes from a second window of
-    # the same length right after, with its class timed.  The timing mask is
-    # part of the captured preconditioner graphs: it is set before the warm-up
-    # so that the capture happens there.
-    mask = (1 << NK) - 1 if args.breakdown else 0
+    arms.set("extrapolated")
+    mask = (1 << NK) - 1 if args.breakdown else (1 << KC_SMOOTH0)
     capi.check(L.wpf_set_kernel_timing(sim.h, mask), "timing")
-    for _ in range(args.spinup + args.warmup):
+    sim.step()   # recaptures the cycle graphs with the timer nodes
+    capi.check(L.wpf_set_kernel_timing(sim.h, mask), "timing")
+    for _ in range(args.steps):
         sim.step()
-    sp = C.c_void_p()
-    capi.check(L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
-    stream = torch.cuda.ExternalStream(sp.value)
-    capi.check(L.wpf_set_kernel_timing(sim.h, mask), "timing")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(dev)
-    clocks.start()
-    n0 = C.c_int64()
-    L.wpf_launch_count(sim.h, C.byref(n0))
-    e0.record(stream)
-    stats = [sim.step() for _ in range(args.steps)]
-    e1.record(stream)
-    torch.cuda.synchronize()
-    n1 = C.c_int64()
-    L.wpf_launch_count(sim.h, C.byref(n1))
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
     kms = (C.c_double * NK)()
     kcnt = (C.c_int64 * NK)()
-    if not args.breakdown:   # the roofline window: the finest-level smoother timed
-        capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
-        sim.step()   # recaptures the cycle graphs with the timer nodes
-        capi.check(L.wpf_set_kernel_timing(sim.h, 1 << KC_SMOOTH0), "timing")
-        for _ in range(args.steps):
-            sim.step()
     L.wpf_kernel_times(sim.h, kms, kcnt, NK)
     capi.check(L.wpf_set_kernel_timing(sim.h, 0), "timing")
-    ms_max = max_over_ranks(ms, world)
-    n = args.n
-    ncell = n ** 3
-    value = job_rate(world, args.steps, ms_max)
-
-    # roofline of the finest-level red-black Gauss-Seidel smoother (the
-    # largest share of the step in the launch list).  A finest level of at
-    # least 2^23 cells runs the one-pass pipelined sweep, whose algorithmic
-    # bytes per cell (FP32) are: couplings cx,cy,cz (12 B) + 1/diag (4 B) +
-    # b (4 B) + the input x (4 B) + the output x (4 B) = 28 B; the zero-guess
-    # first sweep of a cycle reads no input x (24 B); the coarse correction is
-    # a separate prolongation pass before the post-sweeps.  Four sweeps per cycle
-    # (nu = 2 on each side).  Smaller finest levels run two half-sweep
-    # kernels: 20 B/cell each (12 B couplings + 2 B other colour + 6 B b,
-    # 1/diag, new x of this colour), 12 B for the zero-guess one.
-    nu = 2
+    ncell = args.n ** 3
+    # algorithmic bytes per cell of the finest-level sweep (FP32): on levels of
+    # at least 2^23 cells the one-pass pipelined sweep reads the couplings
+    # cx, cy, cz (12 B), 1/diag (4 B), b (4 B) and the input x (4 B) and
+    # writes the output x (4 B): 28 B; the zero-guess first sweep of a cycle
+    # reads no x: 24 B; nu = 2 sweeps per side, four per cycle.  Smaller finest
+    # levels run two half-sweep kernels: 20 B per cell each, 12 B zero-guess.
+    nu = args.nu
     cnt = int(kcnt[KC_SMOOTH0])
     smooth_ms = float(kms[KC_SMOOTH0])
     if ncell >= (1 << 23):
@@ -327,130 +403,122 @@ def run_ours(args):
     if ncell >= (1 << 23):
         tpc = sweep_traffic_per_cell()
         traffic = tpc * ncell if tpc else None
-    roof = {"kernel": kname, "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s",
+    roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
             "traffic_source": "profiles/k_sweep_async_224.md (ncu, 224^3, scaled by cells)",
             "peak_source": peak_kind, "bytes_per_cell_per_launch": per_cell,
             "launches": cnt, "avg_launch_us": smooth_ms * 1000.0 / max(cnt, 1)}
+    breakdown = ({KC_NAMES[c]: float(kms[c]) / args.steps for c in range(NK)}
+                 if args.breakdown else None)
+    return roof, breakdown
 
-    upd_ms = statistics.mean(s.update_ms for s in stats)
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    head = headline_arm(args)
+    arms_list = [a for a in ARMS if not (a == "learned" and args.no_learned)
+                 and not (a == "plain_fp64" and args.no_plain)]
+    # the headline arm is timed last in the last window, under the clock sampler
+    arms_list.sort(key=lambda a: a == head)
+    wins = windows_of(args)
+    case = make_workload(args, rank)
+    arms = Arms(args, case, want_net="learned" in arms_list)
+    if arms.net is None and "learned" in arms_list:
+        arms_list.remove("learned")
+        head = "extrapolated"
+    windows = []
+    head_line = None
+    for wi, w in enumerate(wins):
+        arms.advance_to(w)
+        row = {}
+        clocks = None
+        if wi == len(wins) - 1:   # sampled over the last window's arms, the headline last
+            clocks = ClockSampler(dev)
+            clocks.start()
+        for arm in arms_list:
+            last = wi == len(wins) - 1 and arm == head
+            r = arms.time(arm, world, clocks if last else None)
+            row[arm] = r
+            if last:
+                head_line = r
+        if "plain_fp64" in row:
+            for arm in row:
+                if arm != "plain_fp64":
+                    row[arm]["speedup_vs_plain_fp64"] = row[arm]["value"] / row["plain_fp64"]["value"]
+        windows.append(row)
+    ncell = args.n ** 3
+    value = head_line["value"]
+    roof, breakdown = roofline_window(args, arms)
     out = {
         "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head_line["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian random field permeability; no data set)",
         "config": config_of(args, world),
         "cell_updates_per_s": value * ncell,
-        "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
-        "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
-        "outer_passes_per_step": statistics.mean(s.outer_iterations for s in stats),
-        "relres_max": max(s.relres for s in stats),
-        "fused_update_ms": upd_ms,
-        # (quiescent bricks move no bytes: a cell rate, not an algorithmic GB/s)
-        "fused_update_cell_updates_per_s": ncell / (upd_ms / 1000.0) if upd_ms > 0 else None,
-        "gpu_launches": int(n1.value - n0.value),
-        "launches_before_timed": int(n0.value),   # skip count for a launch list of the timed steps
+        "darcy_solve_ms": head_line["darcy_solve_ms"],
+        "pcg_iterations_per_step": head_line["pcg_iterations_per_step"],
+        "outer_passes_per_step": head_line["outer_passes_per_step"],
+        "relres_max": head_line["relres_max"],
+        "relres0_mean": head_line["relres0_mean"],
+        "fused_update_ms": head_line["fused_update_ms"],
+        "update_active_fraction": head_line["update_active_fraction"],
+        "gpu_launches": head_line["gpu_launches"],
         "roofline": roof,
-        "clocks": clk,
-        "kernel_class_ms": ({KC_NAMES[c]: float(kms[c]) / args.steps for c in range(NK)}
-                            if args.breakdown else {KC_NAMES[3]: smooth_ms / args.steps}),
-        "kernel_class_launches": ({KC_NAMES[c]: int(kcnt[c]) // args.steps for c in range(NK)}
-                                  if args.breakdown else None),
-        "relres0_mean": statistics.mean(s.relres0 for s in stats),
-        "warm_start_used": sum(1 for s in stats if s.warm_start == 1),
-        "warm_start_fallbacks": sum(1 for s in stats if s.warm_start == -1),
+        "clocks": head_line.get("clocks"),
+        "windows": windows,
     }
-    if args.solver == "mixed" and not args.no_plain:
-        out["plain_fp64"] = plain_fp64_pass(args, case, world)
-        out["speedup_vs_plain_fp64"] = value / out["plain_fp64"]["value"]
-    if args.solver == "mixed" and not args.no_learned:
-        out["learned"] = learned_pass(args, case, world)
+    last = windows[-1]
+    if "plain_fp64" in last:
+        out["plain_fp64"] = last["plain_fp64"]
+        out["speedup_vs_plain_fp64"] = value / last["plain_fp64"]["value"]
+    for arm in ("learned", "extrapolated"):
+        if arm in last and arm != head:
+            out[arm] = last[arm]
+    if breakdown:
+        out["kernel_class_ms"] = breakdown
     if not args.no_e2e:
-        out["e2e"] = e2e_pass(args, sim, stream, world)
+        arms.set(head)
+        out["e2e"] = e2e_pass(args, arms.sim, arms.stream(), world)
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            out["cpu_baseline"] = cpu_sample(sim, args)
+            out["cpu_baseline"] = cpu_sample(arms.sim, args)
         except Exception as e:  # the baseline must not sink the GPU line
             out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
-    sim.close()
+    arms.close()
+    if args.kwh_alt > 0:
+        out["kwh_alt"] = alt_kwh_pass(args, rank, world, [a for a in arms_list if a != "learned"])
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
 
 
-def learned_pass(args, case, world):
-    """The same run with the learned correction on top of the extrapolated
-    start (weights trained on 128^3 runs, mizuho_edit_gb300/weights), timed
-    the same way; reports what it changes against the headline run."""
-    import torch
-    from mizuho_edit_gb300 import capi, learned
-    from mizuho_edit_gb300.sim import Simulation
-    path = learned.DEFAULT_WEIGHTS
-    if not os.path.exists(path):
-        return {"unavailable": "no trained weights at mizuho_edit_gb300/weights"}
-    n = args.n
-    net = learned.WarmStartNet(n // 2, n // 2, n // 2)
-    net.set_params(learned.WarmStartNet.load_params(path))
-    kw = solver_kwargs(args)
-    kw["extrapolate"] = True
-    with Simulation(case.params, case.permeab_rock, case.phase, case.concent, **kw) as sim:
-        learned.attach(sim, net)
-        for _ in range(args.spinup + args.warmup):
-            sim.step()
-        sp = C.c_void_p()
-        capi.check(sim.L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
-        stream = torch.cuda.ExternalStream(sp.value)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        stats = [sim.step() for _ in range(args.steps)]
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = max_over_ranks(e0.elapsed_time(e1), world)
-        learned.attach(sim, None)
-    net.close()
-    return {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
-            "ms_per_step": ms / args.steps,
-            "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
-            "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
-            "relres0_mean": statistics.mean(s.relres0 for s in stats),
-            "net_start_kept": sum(1 for s in stats if s.warm_start == 2),
-            "extrapolation_only": sum(1 for s in stats if s.warm_start == 1),
-            "fallbacks_to_previous_pressure": sum(1 for s in stats if s.warm_start == -1),
-            "relres_max": max(s.relres for s in stats)}
-
-
-def plain_fp64_pass(args, case, world):
-    """The plain method on the same input: FP64 MG-PCG to the same 1e-8
-    residual, same warm-up and step count, timed the same way."""
-    import torch
-    from mizuho_edit_gb300 import capi
-    from mizuho_edit_gb300.sim import Simulation
-    with Simulation(case.params, case.permeab_rock, case.phase, case.concent,
-                    **solver_kwargs(args, "fp64")) as sim:
-        for _ in range(args.spinup + args.warmup):
-            sim.step()
-        sp = C.c_void_p()
-        capi.check(sim.L.wpf_get_stream(sim.h, C.byref(sp)), "wpf_get_stream")
-        stream = torch.cuda.ExternalStream(sp.value)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        stats = [sim.step() for _ in range(args.steps)]
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = max_over_ranks(e0.elapsed_time(e1), world)
-    return {"value": job_rate(world, args.steps, ms), "unit": "time-steps/s",
-            "ms_per_step": ms / args.steps,
-            "darcy_solve_ms": statistics.mean(s.solve_ms for s in stats),
-            "pcg_iterations_per_step": statistics.mean(s.inner_iterations for s in stats),
-            "relres_max": max(s.relres for s in stats)}
+def alt_kwh_pass(args, rank, world, arm_names):
+    """The same windows at a second dissolved-rock permeability (kwh): how
+    the numbers move with the contrast between dissolved and intact rock."""
+    case = make_workload(args, rank, kwh=args.kwh_alt)
+    arms = Arms(args, case, want_net=False)
+    rows = []
+    try:
+        for w in windows_of(args):
+            arms.advance_to(w)
+            row = {a: arms.time(a, world) for a in arm_names}
+            if "plain_fp64" in row and "extrapolated" in row:
+                row["extrapolated"]["speedup_vs_plain_fp64"] = (row["extrapolated"]["value"] /
+                                                                row["plain_fp64"]["value"])
+            rows.append(row)
+    finally:
+        arms.close()
+    return {"workload": workload_name(args, args.kwh_alt), "windows": rows}
 
 
 def e2e_pass(args, sim, stream, world):
@@ -541,11 +609,22 @@ def run_reference(args):
     sample = (f"{len(times)} of {args.steps} requested reference time steps at {n}^3 after "
               f"{wdone} warm-up steps (BiCGStab+SOR(10,1.7), rtol 1e-10, {threads} OpenMP "
               f"threads as SOR blocks), {tot:.1f} s")
+    cfg = {"workload": workload_name(args), "grid": [n, n, n],
+           "solver": "BiCGStab + SOR(10 sweeps, omega 1.7) at rtol 1e-10, maxit 1000, from the "
+                     "previous pressure: the reference's PETSc settings (wPFAW3D.f90:616-617, "
+                     "980, 994-1000), host-driven on the CPU (C restatement, OpenMP threads as "
+                     "the SOR blocks of MPI ranks)",
+           "darcy_rtol": 1e-10, "dtype_state": "f64",
+           "timed_steps": f"{wdone + 1}..{wdone + len(times)} of a cold run (the GPU arms time "
+                         f"steps past {windows_of(args)[-1]}; this solver needs 62-72 BiCGStab "
+                         f"iterations per solve at every step observed, early or late, so its "
+                         f"cost per step does not depend on the window)",
+           "parallelism": "single-domain, host cores"}
     out = {"metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": world,
            "steps": len(times), "warmup": wdone, "ms_per_step": 1000.0 * tot / len(times),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Gaussian random field permeability; no data set)",
-           "config": config_of(args, world), "impl": "reference",
+           "config": cfg, "impl": "reference",
            "cell_updates_per_s": v * n ** 3,
            "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": threads, "kind": "port",
                             "sample": sample},

@@ -32,7 +32,7 @@ def _rank(rank, world, port, out_dir):
         ms = 10.0 + 5.0 * rank                      # this rank's timed region
         ms_max = bench.max_over_ranks(ms, world, device="cpu")
         rate = bench.job_rate(world, 10, ms_max)
-        args = argparse.Namespace(n=8, log_var=2.0, corr=2.0, seed=2026)
+        args = argparse.Namespace(n=8, log_var=2.0, corr=2.0, seed=2026, kwh=1000.0)
         case = bench.make_workload(args, rank)   # this rank's replica
         res = {"ms_max": ms_max, "rate": rate, "k_sum": float(np.sum(case.permeab_rock))}
     finally:

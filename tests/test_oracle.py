@@ -207,3 +207,26 @@ def test_golden_vectors(oracle_mod):
     for k in ("pressure", "phase", "concent"):
         assert rel_l2(getattr(s, k), g[k]) < 1e-12, k
     assert s.dtime == pytest.approx(float(g["dtime"]), rel=1e-13)
+
+
+@pytest.mark.parametrize("tfac,steps,stable", [(0.2, 20, False), (0.05, 150, False), (0.025, 150, True)])
+def test_dt_law_stability_limit(oracle_mod, tfac, steps, stable):
+    """Why the cases use tfac = 0.025: the dt law (wPFAW3D.f90:2227-2230) has
+    no stability guard, and the anisotropic phase equation (W up to
+    W0 (1 + eps) = 3 W0 with eps = w, :1298-1310) is explicit-stable only
+    below tfac ~ 0.04 at w = 2, dx = 1.  The suggested 0.2 blows the phase
+    field up within a few steps on the reference's own arithmetic, 0.05
+    within ~100; 0.025 keeps |phase| <= 1."""
+    case = _case((24, 16, 16), seed=5, log_var=1.0, corr_len=3.0, tfac=tfac)
+    s = _sim(oracle_mod, case)
+    worst = 0.0
+    for _ in range(steps):
+        s.step(oracle_mod.SOLVE_CG, 1e-12)
+        m = float(np.max(np.abs(s.phase)))
+        worst = max(worst, m) if np.isfinite(m) else np.inf
+        if worst > 2.0:
+            break
+    if stable:
+        assert worst <= 1.0 + 1e-12
+    else:
+        assert worst > 2.0
