@@ -86,6 +86,9 @@ def parse():
                     help="stage the finest-level sweep with cp.async instead of bulk-tensor copies")
     ap.add_argument("--no-step-graph", action="store_true",
                     help="host-driven steps instead of one graph launch per step")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the ensemble line (48 members: 16 each at 64^3, 96^3, 128^3)")
+    ap.add_argument("--ensemble-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -496,10 +499,32 @@ def run_ours(args):
     arms.close()
     if args.kwh_alt > 0:
         out["kwh_alt"] = alt_kwh_pass(args, rank, world, [a for a in arms_list if a != "learned"])
+    if not args.no_ensemble and world == 1:
+        out["ensemble"] = ensemble_pass(args)
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def ensemble_pass(args):
+    """48 permeability realisations with uneven grids (16 each at 64^3, 96^3,
+    128^3; log-K variance U(0.5, 3), correlation length U(3, 12), Damkohler
+    log-uniform on [1, 100]), FP32-refined solve to 1e-8: launch shapes and
+    solver settings autotuned per grid shape, then every ensemble step one
+    launch of one CUDA graph holding all members (wpf_ensemble_run); timed
+    with a synchronize on both sides."""
+    from mizuho_edit_gb300 import ensemble
+    members = ensemble.make_members((16, 16, 16))
+    tuned = ensemble.autotune(members, spinup=10, steps=4, log=lambda *a: None)
+    res = ensemble.run(members, tuned, args.ensemble_steps, 20, 16, log=lambda *a: None)
+    return {"metric": "ensemble cell-updates/s", "value": res["ensemble_cell_updates_per_s"],
+            "members": res["members"], "shapes": res["shapes"], "steps": res["steps"],
+            "spinup": res["spinup"], "wall_s": res["wall_s"],
+            "member_steps_per_s": res["member_steps_per_s"],
+            "converged_last_step": res["converged_last_step"],
+            "launch": "one CUDA graph launch per ensemble step (all members' steps as branches)",
+            "tuned": ensemble.tuned_table(tuned)}
 
 
 def alt_kwh_pass(args, rank, world, arm_names):

@@ -86,6 +86,10 @@ typedef struct wpf_solver_opts {
     int32_t flags;             /* WPF_SOLVER_NO_GRAPHS: launch each preconditioner
                                   cycle kernel by kernel instead of replaying it as a
                                   captured CUDA graph (same arithmetic)                 */
+    int32_t sweep_zchunk;      /* z planes per block of the pipelined sweep (0: the
+                                  chunk that fills whole waves of resident blocks)      */
+    int32_t row_blocks_per_sm; /* grid of the row-patch kernels (4 x 2 rows of x per
+                                  block, grid-stride) in blocks per SM (0: 8)           */
 } wpf_solver_opts;
 
 #define WPF_SOLVER_NO_GRAPHS 1
@@ -107,9 +111,11 @@ typedef struct wpf_solver_opts {
  * convergence tests on the device (conditional graph nodes: a WHILE node over
  * the refinement passes holding a WHILE node over the PCG iterations) and the
  * fused update, with one read-back per step.  The kernels, their order and so
- * the results are those of the host-driven step.  wpf_ensemble_run then
- * advances all such members in one launch of one graph.  Ignored while
- * kernel timing is on or a warm-start net is attached.                     */
+ * the results are those of the host-driven step.  With a warm-start net
+ * attached (wpf_net.h) its features, forward pass and prolongation are part
+ * of the graph and the step taken along its correction is decided on the
+ * device.  wpf_ensemble_run then advances all such members in one launch of
+ * one graph.  Ignored while kernel timing is on.                           */
 #define WPF_SOLVER_STEP_GRAPH 8
 
 /* Per-step / per-solve statistics. */
@@ -130,7 +136,7 @@ typedef struct wpf_step_stats {
     double relres0;            /* relative residual of the warm start                  */
     int32_t active_cells;      /* cells the fused update evaluated in FP64 (interface and
                                   concentration work lists; the rest were copies)       */
-    int32_t pad;
+    int32_t device_resident;   /* 1: the step ran as one graph launch (STEP_GRAPH)      */
 } wpf_step_stats;
 
 /* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */

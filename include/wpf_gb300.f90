@@ -77,6 +77,8 @@ module wpf_gb300
       integer(c_int64_t) :: sweep_min_cells
       integer(c_int32_t) :: w_from_level
       integer(c_int32_t) :: flags
+      integer(c_int32_t) :: sweep_zchunk
+      integer(c_int32_t) :: row_blocks_per_sm
    end type wpf_solver_opts
 
    type, bind(C) :: wpf_step_stats
@@ -94,7 +96,7 @@ module wpf_gb300
       integer(c_int32_t) :: warm_start
       real(c_double) :: relres0
       integer(c_int32_t) :: active_cells
-      integer(c_int32_t) :: pad
+      integer(c_int32_t) :: device_resident
    end type wpf_step_stats
 
    ! showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux

@@ -54,7 +54,8 @@ class Well(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_outer", C.c_int32), ("max_inner", C.c_int32),
                 ("smooth_sweeps", C.c_int32), ("rtol", C.c_double), ("inner_rtol", C.c_double),
-                ("sweep_min_cells", C.c_int64), ("w_from_level", C.c_int32), ("flags", C.c_int32)]
+                ("sweep_min_cells", C.c_int64), ("w_from_level", C.c_int32), ("flags", C.c_int32),
+                ("sweep_zchunk", C.c_int32), ("row_blocks_per_sm", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -63,7 +64,7 @@ class StepStats(C.Structure):
                 ("taumin", C.c_double), ("dtime", C.c_double), ("max_courant", C.c_double),
                 ("solve_ms", C.c_double), ("update_ms", C.c_double),
                 ("kernel_launches", C.c_int32), ("warm_start", C.c_int32),
-                ("relres0", C.c_double), ("active_cells", C.c_int32), ("pad", C.c_int32)]
+                ("relres0", C.c_double), ("active_cells", C.c_int32), ("device_resident", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -254,7 +254,7 @@ int wpf_set_solver(wpf_handle* h, const wpf_solver_opts* o) {
     if (!h || !o) return WPF_ERR_ARG;
     if (o->mode != WPF_SOLVER_FP64 && o->mode != WPF_SOLVER_MIXED) return WPF_ERR_ARG;
     if (o->max_outer < 0 || o->max_inner < 1 || !(o->rtol > 0) || o->smooth_sweeps < 0 ||
-        o->smooth_sweeps > 16)
+        o->smooth_sweeps > 16 || o->sweep_zchunk < 0 || o->row_blocks_per_sm < 0 || o->row_blocks_per_sm > 64)
         return WPF_ERR_ARG;
     cudaStreamSynchronize(h->stream);
     solver_drop_graphs(h);   // the captured cycles bake in nu, the sweep and W-cycle levels
@@ -700,6 +700,7 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     s->max_courant = umax * dt / p.dx;
     s->kernel_launches = (int32_t)(h->nlaunch - l0);
     s->active_cells = (int32_t)h->last_active;
+    s->device_resident = 0;
     *dtime_inout = dt;
     return srs;
 }

@@ -167,6 +167,7 @@ __global__ void k_step_begin(StepCtl* c, double* dsc, double dt_c, double dt_a) 
     }
     c->bnorm = c->relres = c->relres0 = c->r0 = c->tol = 0.0;
     c->pass = c->outer = c->inner = c->it = c->need_pcg = c->accept = c->used = c->pcgs = 0;
+    c->alpha = 0.f;
     c->status = WPF_ERR_NOT_CONVERGED;
     for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;   // RR64 BB64 RR0WS RW WW
     dsc[S_WSS2] = 0.0;
@@ -188,7 +189,7 @@ static bool ws_enabled(const wpf_handle* h) { return (h->opts.flags & WPF_SOLVER
 bool step_graph_ready(const wpf_handle* h, int itime) {
     const int f = h->opts.flags;
     return (f & WPF_SOLVER_STEP_GRAPH) && !(f & WPF_SOLVER_NO_GRAPHS) && itime >= 3 && h->timing_mask == 0 &&
-           !h->ws_net && h->opts.max_outer >= 1 && h->have_wells && h->ndir > 0 &&
+           h->opts.max_outer >= 1 && h->have_wells && h->ndir > 0 &&
            (!ws_enabled(h) || h->ws_hist == 2);
 }
 
@@ -206,6 +207,7 @@ int step_graph_prepare(wpf_handle* h) {
         WPF_CUDA(cudaMallocHost((void**)&h->gdsc_host, S_COUNT * sizeof(double)));
         h->gctl_dirty = true;
     }
+    if (h->ws_net && ws_enabled(h) && (rc = ws_net_prepare(h))) return rc;
     if (!h->cap_split) WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_split, cudaStreamNonBlocking));
     if (!h->cap_ws) {
         WPF_CUDA(cudaStreamCreateWithFlags(&h->cap_ws, cudaStreamNonBlocking));
@@ -325,6 +327,10 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter;
     h->nlaunch += launches;
     int rc = c.status;
+    if (h->ws_net && ws_enabled(h) && rc != WPF_ERR_CUDA) {   // the net's kernels' bounded waits
+        const int nrc = ws_net_check(h);
+        if (nrc) rc = nrc;
+    }
     if (kerr) {   // a sweep whose bounded staging wait ran out left its flag
         WPF_CUDA(cudaMemsetAsync(h->dsc + S_KERR, 0, sizeof(double), h->stream));
         WPF_CUDA(cudaStreamSynchronize(h->stream));
@@ -349,6 +355,7 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
         st->max_courant = umax * c.dt / h->prm.dx;
         st->kernel_launches = (int32_t)launches;
         st->active_cells = (int32_t)h->last_active;
+        st->device_resident = 1;
     }
     cudaGetLastError();
     if (dt_out) *dt_out = c.dt;
@@ -371,6 +378,8 @@ void step_graph_key(const wpf_handle* h, const void** k) {
     k[7] = h->bact_ok ? h->bact[0] : nullptr;
     // the level-0 build rebuilds only the cells of recomputed faces
     k[8] = (h->t_from_prev && l0_incremental(h)) ? h->l0mark : nullptr;
+    // the learned correction of the start, when a net is attached
+    k[9] = ws ? (const void*)h->ws_net : nullptr;
 }
 
 // Upload the increment step sizes when the host-driven path changed them.

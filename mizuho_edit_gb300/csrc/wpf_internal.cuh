@@ -97,6 +97,14 @@ struct SweepMaps {
     CUtensorMap x, cx, cy, cz, id, b;
 };
 
+// cuTensorMapEncodeTiled, fetched once through the runtime's driver entry
+// points (the library links the runtime only); nullptr when unavailable.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder();
+
 // Control block of the device-resident step (WPF_SOLVER_STEP_GRAPH): the
 // decisions the host-driven step takes after each read-back, taken instead by
 // one-thread kernels inside the step graph.  Copied back once per step.
@@ -104,6 +112,8 @@ struct StepCtl {
     double dt;               // this step's dt (the dt law on the device)
     double h1, h2;           // step sizes of the last two increments
     float wa, wb;            // extrapolation coefficients e = wa d1 + wb d2
+    float alpha;             // step of the learned correction (0: none taken)
+    float alpha_pad;
     double bnorm, relres, relres0;
     double r0, tol;          // PCG: ||r_0|| and the relative tolerance of this pass
     int pass;                // refinement pass whose residual was taken last
@@ -138,7 +148,7 @@ int gb_handle(GraphBuilder& b, cudaGraphConditionalHandle* hd);
 int gb_cond(GraphBuilder& b, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hd,
             GraphBuilder* body);
 
-constexpr int STEP_KEY = 9;   // buffer pointers and modes a captured step depends on
+constexpr int STEP_KEY = 10;  // buffer pointers and modes a captured step depends on
 constexpr int BRICK_X = 32, BRICK_Y = 4, BRICK_Z = 2;   // fused-update bricks (one RB-thread block)
 
 // Kernels launched per step by a captured device-resident step:
@@ -223,6 +233,7 @@ struct wpf_handle {
     double* staging;         // dense halo-array staging for host copies (lazily allocated)
     bool host_pageable_direct;   // kernels reach pageable host memory in place (host page tables)
     struct wpf_net* ws_net;  // learned warm start (not owned), or null
+    const struct wpf_net* ws_net_warm;   // the net whose kernels ran once outside a capture
     float* ws_e[2];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output)
     uint16_t* ws_in;         // net input (bf16, net grid, 16 channels)
     float* ws_out;           // net output channel 0 (net grid)
@@ -535,7 +546,8 @@ constexpr int RB = 256;
                  i = (j <= (g).ny && k <= (g).nz) ? 1 + lane_ : (g).nx + 1;                \
              i <= (g).nx; i += 32)
 
-inline unsigned row_blocks(const wpf_handle* h, const Grid& g, int per_sm = 8) {
+inline unsigned row_blocks(const wpf_handle* h, const Grid& g, int per_sm = 0) {
+    if (per_sm <= 0) per_sm = h->opts.row_blocks_per_sm > 0 ? h->opts.row_blocks_per_sm : 8;
     const long long patches = (long long)((g.ny + 3) / 4) * ((g.nz + 1) / 2);
     const long long cap = (long long)h->nsm * per_sm;
     return (unsigned)(patches < cap ? patches : cap);
@@ -600,6 +612,14 @@ int step_graph_prepare(wpf_handle* h);           // allocations a capture needs
 int step_graph_capture(wpf_handle* h, GraphBuilder& b, StepCounts* n);
 int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, double* dt_out);
 int step_graph_run(wpf_handle* h, wpf_step_stats* st, double* dt_out);
+// The learned start inside a captured step: features, forward pass and
+// prolongation of the attached net on stream s, with no synchronisation
+// (ws_net_prepare, outside any capture, allocates the buffers, takes the
+// log-K statistics and runs the net's kernels once); ws_net_check reads the
+// net's bounded-wait error flag after the step.
+int ws_net_prepare(wpf_handle* h);
+int ws_net_capture(wpf_handle* h, cudaStream_t s);
+int ws_net_check(wpf_handle* h);
 void step_graph_key(const wpf_handle* h, const void** k);   // STEP_KEY buffer pointers
 int step_graph_sync_ctl(wpf_handle* h);          // upload host-side history if stale
 void step_graphs_drop(wpf_handle* h);

@@ -249,6 +249,160 @@ __global__ void __launch_bounds__(CT) k_conv3d(ConvArgs a) {
     if (warp == 0) tmem_dealloc(tmem, NCOL);
 }
 
+// ---- row-tiled convolution of 16-channel inputs, staged by TMA ----------------
+// For a level whose nx is a multiple of TX (128, 64, 32 or 16) and whose ny
+// is a multiple of TY = 128 / TX, a CTA owns the TX x TY x 1 brick of output
+// voxels (x0.., y0.., z0): M = 128 rows in x-fastest order, N = COUT.  Its
+// input halo -- 3 z planes x (TY + 2) rows x the brick's x range, both
+// 8-channel halves -- is staged once by bulk-tensor copies that fill zeros
+// outside the grid (the convolution's zero padding), each half in its own
+// "chunk plane" so that 8 consecutive x voxels form one 128-byte core matrix
+// of the no-swizzle K-major layout.  Every tap's A operand is then a window
+// of that plane: the descriptor's start moves by (dz, dy) rows and, with TY = 1
+// (one 130-voxel row), by dx voxels; with TY > 1 the rows of the window must
+// be TX apart, so three copies shifted by dx = -1, 0, 1 are staged instead.
+// All 27 taps' weights sit in shared memory as B operands; one thread issues
+// the 27 MMAs (K = 16 each) back to back and commits them to an mbarrier.
+// No per-tap gather and no per-tap block barrier: the 16-channel layers (the
+// finest level of the U-Net) were latency-bound on exactly those.
+template <int COUT, int TX>
+struct RowTile {
+    static constexpr int TY = 128 / TX;
+    static constexpr bool SHIFT = TY > 1;
+    static constexpr int BOXX = SHIFT ? TX : TX + 2;       // x extent of one staged box
+    static constexpr int NSH = SHIFT ? 3 : 1;              // staged dx copies
+    static constexpr int ROWS = 3 * (TY + 2);               // (z, y) rows of a box
+    static constexpr int CH = ROWS * BOXX * 16;             // bytes of one box (8 channels)
+    static constexpr int CHP = (CH + 127) / 128 * 128;      // its slot (128-byte aligned)
+    static constexpr int ABYTES = NSH * 2 * CHP;
+    static constexpr int BBYTES = 27 * 2 * COUT * 16;
+    static constexpr int SMEM = ABYTES + BBYTES + 1024;
+    static_assert(TX % 8 == 0 && TX * TY == 128, "a brick is 128 voxels, whole core matrices in x");
+    static_assert(SMEM <= 200 * 1024, "row conv stage exceeds the shared allocation");
+};
+
+struct RowConvArgs {
+    int nx, ny, nz;
+    const bf16_t* w;
+    const float* bias;
+    bf16_t* out16;
+    float* out32;
+    int relu;
+    int* err;
+};
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int COUT, int TX>
+__global__ void __launch_bounds__(CT) k_conv3d_row(RowConvArgs a, const __grid_constant__ CUtensorMap in_map) {
+    using T = RowTile<COUT, TX>;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint64_t bar[2];   // 0: the input halo landed; 1: the MMAs finished
+    __shared__ uint32_t tmem_sh;
+    constexpr uint32_t NCOL = 32;
+    constexpr uint32_t IDESC = idesc_bf16(128, COUT);
+    static_assert(COUT == 16 || COUT == 32, "row conv: N = 16 or 32");
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int ntx = a.nx / TX, nty = a.ny / T::TY;
+    const int bx = blockIdx.x % ntx, by = (blockIdx.x / ntx) % nty, bz = blockIdx.x / (ntx * nty);
+    const int x0 = bx * TX, y0 = by * T::TY, z0 = bz;
+    unsigned char* Bs = sm + T::ABYTES;
+    if (warp == 0) tmem_alloc(&tmem_sh, NCOL);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (tid == 0) {
+        mbar_expect_tx(&bar[0], (uint32_t)(T::NSH * 2 * T::CH));
+        for (int sh = 0; sh < T::NSH; ++sh)
+            for (int c = 0; c < 2; ++c)
+                tma_load_4d(sm + (sh * 2 + c) * T::CHP, &in_map, 8 * c, T::SHIFT ? x0 + sh - 1 : x0 - 1, y0 - 1,
+                            z0 - 1, &bar[0]);
+    }
+    // the 27 taps' weights as B operands: tap t, channel half c, row co
+    for (int q = tid; q < 27 * 2 * COUT; q += CT) {
+        const int t = q / (2 * COUT), r = q - t * (2 * COUT), c = r / COUT, co = r - c * COUT;
+        const uint4 val = reinterpret_cast<const uint4*>(a.w + ((long long)co * 27 + t) * 16)[c];
+        *reinterpret_cast<uint4*>(Bs + t * (2 * COUT * 16) + c * (COUT * 16) + (co >> 3) * 128 + (co & 7) * 16) =
+            val;
+    }
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = tmem_sh;
+    const uint32_t sbase = smem_u32(sm);
+    bool ok = true;
+    if (tid == 0) {
+        if (!mbar_wait(&bar[0], 0)) ok = false;
+        tc_after();
+        if (ok) {
+            for (int t = 0; t < 27; ++t) {
+                const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;   // 0..2 (offset + 1)
+                const uint32_t arow = (uint32_t)((dz * (T::TY + 2) + dy) * T::BOXX * 16);
+                const uint32_t aoff = T::SHIFT ? (uint32_t)(dx * 2 * T::CHP) + arow : arow + (uint32_t)(dx * 16);
+                const uint64_t ad = sdesc(sbase + aoff, T::CHP, 128);
+                const uint64_t bd = sdesc(sbase + T::ABYTES + t * (2 * COUT * 16), COUT * 16, 128);
+                mma_bf16(tmem, ad, bd, IDESC, t > 0 ? 1u : 0u);
+            }
+        }
+        mma_commit(&bar[1]);   // arrives when every MMA issued above has finished (or at once)
+    }
+    __syncwarp();
+    if (!mbar_wait(&bar[1], 0)) ok = false;
+    tc_after();
+    const int x = x0 + tid % TX, y = y0 + tid / TX;
+    const long long v = ((long long)z0 * a.ny + y) * a.nx + x;
+#pragma unroll
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+        float acc[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
+        if (ok) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                float s = acc[i] + (a.bias ? a.bias[c0 + i] : 0.f);
+                if (a.relu) s = fmaxf(s, 0.f);
+                acc[i] = s;
+            }
+            if (a.out16) {
+                uint4* dst = reinterpret_cast<uint4*>(a.out16 + v * COUT + c0);
+                dst[0] = make_uint4(pack2(acc[0], acc[1]), pack2(acc[2], acc[3]), pack2(acc[4], acc[5]),
+                                    pack2(acc[6], acc[7]));
+                dst[1] = make_uint4(pack2(acc[8], acc[9]), pack2(acc[10], acc[11]), pack2(acc[12], acc[13]),
+                                    pack2(acc[14], acc[15]));
+            } else {
+                float4* dst = reinterpret_cast<float4*>(a.out32 + v * COUT + c0);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+            }
+        }
+    }
+    if (!ok) {   // a wait ran out: the copies and MMAs in flight get a second bounded wait
+        mbar_wait(&bar[0], 0);
+        mbar_wait(&bar[1], 0);
+        atomicExch(a.err, 1);
+    }
+    tc_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, NCOL);
+}
+
 // Weight gradient: D[r][co] = sum_v x[v + d_t][ci] gy[v][co], r = t*CIN + ci.
 // CTA (blockIdx.x = 128-row tile of r, blockIdx.y = chunk of WG_VOX voxels);
 // stages of 32 voxels (two MMAs of K = 16), FP32 atomics into gw.
@@ -570,7 +724,54 @@ static int launch_conv_t(const ConvArgs& a, cudaStream_t s) {
     return WPF_OK;
 }
 
+// The row-tiled kernel on its brick grid; WPF_ERR_CUDA when the tensor map
+// cannot be encoded (the caller then uses the gather kernel).
+template <int COUT, int TX>
+static int launch_conv_row(const ConvArgs& a, cudaStream_t s) {
+    using T = RowTile<COUT, TX>;
+    static bool attr = false;
+    if (!attr) {
+        WPF_CUDA(cudaFuncSetAttribute(k_conv3d_row<COUT, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      T::SMEM));
+        attr = true;
+    }
+    const EncodeTiledFn f = tensor_map_encoder();
+    if (!f) return WPF_ERR_CUDA;
+    CUtensorMap m;
+    const cuuint64_t dims[4] = {16, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)a.nz};
+    const cuuint64_t strides[3] = {32, (cuuint64_t)a.nx * 32, (cuuint64_t)a.nx * a.ny * 32};
+    const cuuint32_t box[4] = {8, (cuuint32_t)T::BOXX, (cuuint32_t)(T::TY + 2), 3};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (f(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.in, dims, strides, box, es,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return WPF_ERR_CUDA;
+    RowConvArgs r;
+    r.nx = a.nx; r.ny = a.ny; r.nz = a.nz;
+    r.w = a.w; r.bias = a.bias; r.out16 = a.out16; r.out32 = a.out32; r.relu = a.relu; r.err = a.err;
+    const unsigned grid = (unsigned)((a.nx / TX) * (a.ny / T::TY) * a.nz);
+    k_conv3d_row<COUT, TX><<<grid, CT, T::SMEM, s>>>(r, m);
+    WPF_CUDA(cudaGetLastError());
+    return WPF_OK;
+}
+
+template <int COUT>
+static int try_conv_row(const ConvArgs& a, cudaStream_t s, bool* done) {
+    *done = true;
+#define WPF_ROW_CASE(TX) \
+    if (a.nx % TX == 0 && a.ny % (128 / TX) == 0) return launch_conv_row<COUT, TX>(a, s);
+    WPF_ROW_CASE(128) WPF_ROW_CASE(64) WPF_ROW_CASE(32) WPF_ROW_CASE(16)
+#undef WPF_ROW_CASE
+    *done = false;
+    return WPF_OK;
+}
+
 static int launch_conv(int cin, int cout, const ConvArgs& a, cudaStream_t s) {
+    if (cin == 16 && (cout == 16 || cout == 32) && (long long)a.nx * a.ny * a.nz == a.nvox) {
+        bool done = false;
+        const int rc = cout == 16 ? try_conv_row<16>(a, s, &done) : try_conv_row<32>(a, s, &done);
+        if (done) return rc;
+    }
 #define WPF_CONV_CASE(I, O) \
     if (cin == I && cout == O) return launch_conv_t<I, O>(a, s);
     WPF_CONV_CASE(16, 16) WPF_CONV_CASE(16, 32) WPF_CONV_CASE(32, 64) WPF_CONV_CASE(64, 64)
@@ -1135,6 +1336,54 @@ int ws_net_correction(wpf_handle* h) {
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
+
+// The device-resident step's learned start.  Buffers, the log-K statistics
+// and one run of the net's kernels (their function attributes are set on the
+// first launch) happen here, outside any stream capture.
+int ws_net_prepare(wpf_handle* h) {
+    const Grid& g = h->g;
+    cudaStream_t s = h->stream;
+    const long long nv = (long long)(g.nx / 2) * (g.ny / 2) * (g.nz / 2);
+    int rc;
+    if (!h->ws_in && (rc = dev_alloc(h, (void**)&h->ws_in, sizeof(uint16_t) * nv * 16))) return rc;
+    if (!h->ws_out && (rc = dev_alloc(h, (void**)&h->ws_out, sizeof(float) * nv))) return rc;
+    if (!h->ws_e[1] && (rc = dev_alloc(h, (void**)&h->ws_e[1], sizeof(float) * g.total))) return rc;
+    if (!h->ws_klog_ready) {
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KLOG0, 0, 2 * sizeof(double), s));
+        WPF_LAUNCH(h, KC_OTHER, net::k_klog_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->krock, h->dsc));
+        h->ws_klog_ready = true;
+    }
+    if (h->ws_net_warm != h->ws_net) {
+        if ((rc = wpf_net_forward(h->ws_net, h->ws_in, h->ws_out, (void*)s))) return rc;
+        h->ws_net_warm = h->ws_net;
+    }
+    return WPF_OK;
+}
+
+// e_net for a captured step: the kernels of ws_net_correction on stream s,
+// with no read-back (the net's error flag is read after the step).
+int ws_net_capture(wpf_handle* h, cudaStream_t s) {
+    const Grid& g = h->g;
+    const int nxn = g.nx / 2, nyn = g.ny / 2, nzn = g.nz / 2;
+    const long long nv = (long long)nxn * nyn * nzn;
+    if (!h->ws_in || !h->ws_out || !h->ws_e[1] || !h->ws_klog_ready) return WPF_ERR_ARG;
+    WPF_CUDA(cudaMemsetAsync(h->dsc + S_DPH2, 0, sizeof(double), s));
+    WPF_LAUNCH(h, KC_OTHER, net::k_dphase_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->phase, h->phase_n, h->dsc));
+    WPF_LAUNCH(h, KC_OTHER, net::k_ws_features<<<net::ew_grid(nv), 256, 0, s>>>(
+        g, nxn, nyn, nzn, h->krock, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc,
+        h->ws_in));
+    wpf_net* n = h->ws_net;
+    int rc = forward(n, h->ws_in, s);
+    if (rc) return rc;
+    k_channel0<<<ew_grid(n->nvox[0]), 256, 0, s>>>(n->out32, 16, (int)n->nvox[0], h->ws_out);
+    h->nlaunch += 2 * WPF_NET_LAYERS + 1;   // the net's kernels (convolutions, pooling, copies)
+    WPF_LAUNCH(h, KC_OTHER, net::k_ws_prolong<<<row_blocks(h, g), RB, 0, s>>>(
+        g, nxn, nyn, nzn, h->ws_out, h->flags, h->dsc, h->ws_e[1]));
+    WPF_CUDA(cudaGetLastError());
+    return WPF_OK;
+}
+
+int ws_net_check(wpf_handle* h) { return h->ws_net ? check_err(h->ws_net, h->stream) : WPF_OK; }
 
 }  // namespace wpf
 

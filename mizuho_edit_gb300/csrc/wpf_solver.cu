@@ -39,6 +39,8 @@
 // the levels of at most 4096 cells run their whole sub-cycle in one block.
 #include <cuda.h>   // CUtensorMap (the encoder is fetched at run time)
 #include <math.h>
+
+#include <mutex>
 #include <stddef.h>
 #include <stdio.h>
 
@@ -1273,16 +1275,10 @@ constexpr long long BIG_CELLS = 1LL << 23;   // default: levels swept by the pip
 // place; the levels from the first one with at most bottom_cells<R>() cells
 // run in one k_bottom block.
 // ---- bulk-tensor maps of the sweep -------------------------------------------------
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
-                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
-                                  CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn tensor_map_encoder() {
+EncodeTiledFn tensor_map_encoder() {
     static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static std::once_flag once;
+    std::call_once(once, [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
@@ -1291,7 +1287,7 @@ static EncodeTiledFn tensor_map_encoder() {
             fn = (EncodeTiledFn)p;
         else
             cudaGetLastError();
-    }
+    });
     return fn;
 }
 
@@ -1374,7 +1370,8 @@ static void launch_sweep(wpf_handle* h, Hierarchy<R>& H, int l, int cls, bool ze
     const SweepMaps& m = H.tm[l][in == L.x ? 1 : 0];
     int* err = reinterpret_cast<int*>(h->dsc + S_KERR);
     const size_t sm = sweep_smem<R>();
-    const int szc = sweep_chunk<R>(h, g);
+    const int szc = h->opts.sweep_zchunk > 0 ? (h->opts.sweep_zchunk < g.nz ? h->opts.sweep_zchunk : g.nz)
+                                             : sweep_chunk<R>(h, g);
     const dim3 gr = sweep_grid(g, szc);
     if (tma && zero)
         WPF_LAUNCH(h, cls, k_sweep_async<R, true, true><<<gr, sb, sm, s>>>(
@@ -1895,6 +1892,52 @@ __global__ void k_ctl_accept(StepCtl* c, double* dsc) {
     }
 }
 
+// The same with a learned correction e_net (S_RW = r_ext.A'e_net, S_WW =
+// |A'e_net|^2): the step alpha = RW / WW that minimises the residual along
+// it, taken when positive; the start (extrapolation + alpha e_net) is kept when
+// its residual is below that of p.  The arithmetic of solve_impl's pass 0.
+__global__ void k_ctl_accept_net(StepCtl* c, double* dsc) {
+    if (threadIdx.x) return;
+    double rstart = dsc[S_RR64];
+    const double r0 = dsc[S_RR0WS], rw = dsc[S_RW], ww = dsc[S_WW];
+    float alpha = 0.f;
+    if (ww > 0.0 && rw > 0.0 && rw == rw) {
+        alpha = (float)(rw / ww);
+        rstart = fmax(rstart - rw * rw / ww, 0.0);
+    }
+    if (rstart <= r0 && rstart == rstart) {
+        c->accept = 1;
+        c->used = alpha > 0.f ? 2 : 1;
+        c->alpha = alpha > 0.f ? alpha : 0.f;
+        dsc[S_RR64] = rstart;
+    } else {
+        c->accept = 0;
+        c->used = -1;
+        c->alpha = 0.f;
+        for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;
+    }
+}
+
+// k_ws_take_net with the decision and the step read from the control block.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_ws_take_net_dev(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
+                                                        const R* __restrict__ cz, const R* __restrict__ diag,
+                                                        const uint8_t* __restrict__ fl, const StepCtl* c,
+                                                        const float* __restrict__ e2, R* __restrict__ r,
+                                                        float* __restrict__ dnew) {
+    __shared__ float salpha;
+    if (threadIdx.x == 0) salpha = (c->accept && c->alpha > 0.f) ? c->alpha : 0.f;
+    __syncthreads();
+    const float alpha = salpha;
+    if (!(alpha > 0.f)) return;
+    const long long sy = g.P, sz = g.S;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        dnew[n] += alpha * e2[n];
+        if (!(fl[n] & F_DIR)) r[n] -= (R)alpha * apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+    }
+}
+
 // After a refinement pass's residual: the pass logic of solve_impl.
 __global__ void k_ctl_pass(StepCtl* c, const double* dsc, double rtol, double inner_rtol, int max_outer,
                            int mixed, cudaGraphConditionalHandle h_pass) {
@@ -1963,25 +2006,30 @@ __global__ void k_ctl_advance(StepCtl* c, double* dsc) {
     for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;
 }
 
-// p += x (when this pass ran PCG iterations) + e1 (when the accepted start is
-// pending); dnew accumulates x.  The arithmetic of k_add_correction(_ws).
+// p += x (when this pass ran PCG iterations) + e1 [+ alpha e2] (when the
+// accepted start is pending; e2 the learned correction, taken when alpha > 0);
+// dnew accumulates x.  The arithmetic of k_add_correction(_ws).
 template <typename R>
 __global__ void __launch_bounds__(RB) k_add_correction_dev(Grid g, double* __restrict__ pr,
                                                            const R* __restrict__ x,
                                                            const float* __restrict__ e1,
+                                                           const float* __restrict__ e2,
                                                            float* __restrict__ dnew, const StepCtl* c) {
     __shared__ int suse;
+    __shared__ float salpha;
     if (threadIdx.x == 0) {
         const bool ok = c->status != WPF_ERR_NONFINITE;
         suse = (ok && c->need_pcg && c->it > 0 ? 1 : 0) | (ok && e1 && c->accept ? 2 : 0);
+        salpha = (e2 && c->alpha > 0.f) ? c->alpha : 0.f;
     }
     __syncthreads();
     const int use = suse;
+    const float alpha = salpha;
     if (!use) return;
     ROW_LOOP_U4(g) {
         const long long n = g.at(i, j, k);
         double inc = (use & 1) ? to_f64<R>(x[n]) : 0.0;
-        if (use & 2) inc += f32_to_f64(e1[n]);
+        if (use & 2) inc += f32_to_f64(alpha > 0.f ? e1[n] + alpha * e2[n] : e1[n]);
         pr[n] += inc;
         if ((use & 1) && dnew) dnew[n] += to_f32<R>(x[n]);
     }
@@ -1994,6 +2042,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     const unsigned rb = row_blocks(h, g);
     const int mixed = h->opts.mode == WPF_SOLVER_MIXED;
     const bool ws_on = (h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && h->ws[0] && h->ws_e[0];
+    const bool net = ws_on && h->ws_net && h->ws_hist >= 2;
     const int nu = h->opts.smooth_sweeps > 0 ? h->opts.smooth_sweeps : 2;
     StepCtl* c = h->gctl;
     double* d = h->dsc;
@@ -2022,11 +2071,18 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
             WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
                                                                        d, &c->wa));
         }
+        if (net && (rc = ws_net_capture(h, s))) return rc;   // e_net in ws_e[1]
         auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
         WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
             g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
-            h->ws_e[0], nullptr, H.r, dnew, d, rk_in));
-        WPF_LAUNCH(h, KC_OTHER, k_ctl_accept<<<1, 32, 0, s>>>(c, d));
+            h->ws_e[0], net ? h->ws_e[1] : nullptr, H.r, dnew, d, rk_in));
+        if (net) {
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_accept_net<<<1, 32, 0, s>>>(c, d));
+            WPF_LAUNCH(h, KC_RESID64, k_ws_take_net_dev<R><<<rb, RB, 0, s>>>(
+                g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags, c, h->ws_e[1], H.r, dnew));
+        } else {
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_accept<<<1, 32, 0, s>>>(c, d));
+        }
         WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                                    h->flags, h->qterm, resid_dsum(h), H.r, d, 1, &c->accept,
                                                                    dnew, rk));
@@ -2068,7 +2124,8 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     if ((rc = gb_begin(pass))) return rc;
     const long long l2 = h->nlaunch;
     WPF_LAUNCH(h, KC_VEC, k_add_correction_dev<R><<<rb, RB, 0, s>>>(g, h->pressure, H.x,
-                                                                    ws_on ? h->ws_e[0] : nullptr, dnew, c));
+                                                                    ws_on ? h->ws_e[0] : nullptr,
+                                                                    net ? h->ws_e[1] : nullptr, dnew, c));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_advance<<<1, 32, 0, s>>>(c, d));
     WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                                h->flags, h->qterm, resid_dsum(h), H.r, d, 0,

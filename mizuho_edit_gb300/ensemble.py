@@ -8,9 +8,19 @@ solver loops are conditional nodes), so that small grids -- whose kernels are
 too short to fill 152 SMs -- overlap on the device with no host round trip;
 before that (the first steps) a pool of host threads steps the members, each
 on its own stream.  Before the timed run, an
-autotuner picks, per grid shape, the solver configuration (multigrid cycle
+autotuner picks, per grid shape, the solver configuration and the launch shapes (multigrid cycle
 shape, the level size from which the pipelined sweep kernel is used,
-smoothing sweeps) with the best measured time per step.
+smoothing sweeps, the sweep's z planes per block, the row-patch kernels'
+blocks per SM) with the best measured time per step.
+
+Why one graph launch per ensemble step rather than one persistent kernel:
+every PCG iteration of every member ends in a reduction that decides the next
+launch, so a persistent kernel would need a grid-wide barrier per solver phase
+of each member and one block shape for kernels whose best shapes differ
+(32x8 sweep tiles, 128-row patches, the one-block bottom cycle); the graph
+keeps each kernel's own launch shape, turns the decisions into conditional
+nodes evaluated on the device and still costs one launch and one
+synchronisation per ensemble step.
 
     python -m mizuho_edit_gb300.ensemble [--members 16,16,16] [--steps 20]
 """
@@ -28,8 +38,12 @@ from .cases import make_case
 from .sim import Simulation
 
 SHAPES = ((64, 64, 64), (96, 96, 96), (128, 128, 128))
-# candidate solver configurations: (W-cycle from level, pipelined-sweep threshold, sweeps per side)
-CANDIDATES = [(2, 0, 2), (1, 0, 2), (3, 0, 2), (2, 1 << 18, 2), (1, 1 << 18, 2), (2, 0, 3)]
+# candidate solver configurations: (W-cycle from level, pipelined-sweep threshold, sweeps per
+# side, z planes per block of the pipelined sweep (0: the wave-filling chunk), row-patch blocks
+# per SM (0: 8))
+CANDIDATES = [(2, 0, 2, 0, 0), (1, 0, 2, 0, 0), (3, 0, 2, 0, 0), (2, 0, 3, 0, 0),
+              (2, 1 << 18, 2, 0, 0), (1, 1 << 18, 2, 0, 0), (2, 1 << 18, 2, 16, 0), (2, 1 << 18, 2, 32, 0),
+              (2, 0, 2, 0, 4), (2, 0, 2, 0, 16)]
 
 
 def make_members(counts=(16, 16, 16), seed: int = 48):
@@ -48,8 +62,9 @@ def make_members(counts=(16, 16, 16), seed: int = 48):
 
 
 def _opts(c):
-    w, thr, nu = c
-    return dict(w_from_level=w, sweep_min_cells=thr, smooth_sweeps=nu)
+    w, thr, nu, zc, rb = c
+    return dict(w_from_level=w, sweep_min_cells=thr, smooth_sweeps=nu, sweep_zchunk=zc,
+                row_blocks_per_sm=rb)
 
 
 def _sim(shape, kw, opts, step_graph=False):
@@ -123,6 +138,16 @@ def run(members, tuned, steps: int, spinup: int, threads: int, log=print, step_g
             s.close()
 
 
+def tuned_table(tuned):
+    """The autotuner's choice per shape, JSON-ready."""
+    if not tuned:
+        return None
+    return {str(k): {"w_from_level": v[0][0], "sweep_min_cells": v[0][1], "smooth_sweeps": v[0][2],
+                     "sweep_zchunk": v[0][3], "row_blocks_per_sm": v[0][4],
+                     "ms_per_step": {str(c): t for c, t in v[1].items()}}
+            for k, v in tuned.items()}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--members", default="16,16,16")
@@ -141,9 +166,7 @@ def main(argv=None):
     if not a.host_steps:   # the thread-pool form on the same members, for comparison
         res["host_threaded_cell_updates_per_s"] = run(
             members, tuned, a.steps, a.spinup, a.threads, step_graph=False)["ensemble_cell_updates_per_s"]
-    res["tuned"] = ({str(k): {"w_from_level": v[0][0], "sweep_min_cells": v[0][1], "smooth_sweeps": v[0][2],
-                              "ms_per_step": {str(c): t for c, t in v[1].items()}}
-                     for k, v in tuned.items()} if tuned else None)
+    res["tuned"] = tuned_table(tuned)
     # the same members one after the other on one thread, for comparison
     if not a.no_tune:
         seq = run(members, tuned, max(a.steps // 4, 2), a.spinup, 1, step_graph=False)

@@ -35,7 +35,8 @@ class Simulation:
                  solver: str = "fp64", rtol: float = 1e-8, inner_rtol: float = 1e-4,
                  max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2,
                  sweep_min_cells: int = 0, w_from_level: int = 0, graphs: bool = True,
-                 extrapolate: bool = False, tma: bool = True, step_graph: bool = False):
+                 extrapolate: bool = False, tma: bool = True, step_graph: bool = False,
+                 sweep_zchunk: int = 0, row_blocks_per_sm: int = 0):
         self.L = capi.load()
         self.params = p = params
         if p.tfac is None:
@@ -53,7 +54,8 @@ class Simulation:
         self.set_solver(solver, rtol, inner_rtol=inner_rtol, max_inner=max_inner,
                         max_outer=max_outer, smooth_sweeps=smooth_sweeps,
                         sweep_min_cells=sweep_min_cells, w_from_level=w_from_level,
-                        graphs=graphs, extrapolate=extrapolate, tma=tma, step_graph=step_graph)
+                        graphs=graphs, extrapolate=extrapolate, tma=tma, step_graph=step_graph,
+                        sweep_zchunk=sweep_zchunk, row_blocks_per_sm=row_blocks_per_sm)
         # initial fields exactly as loadConfig builds them (wPFAW3D.f90:464-496)
         sh = self.halo_shape
         kr = np.full(sh, p.init_permeab, order="F")
@@ -102,21 +104,24 @@ class Simulation:
     def set_solver(self, mode: str = "fp64", rtol: float = 1e-8, inner_rtol: float = 1e-4,
                    max_inner: int = 500, max_outer: int = 20, smooth_sweeps: int = 2,
                    sweep_min_cells: int = 0, w_from_level: int = 0, graphs: bool = True,
-                   extrapolate: bool = False, tma: bool = True, step_graph: bool = False):
+                   extrapolate: bool = False, tma: bool = True, step_graph: bool = False,
+                   sweep_zchunk: int = 0, row_blocks_per_sm: int = 0):
         """Solver options (wpf_set_solver); graphs=False launches every
         preconditioner cycle kernel by kernel instead of replaying a CUDA graph;
         extrapolate=True starts each solve from the pressure extrapolated in
         time (with the fallback to the previous pressure); tma=False stages the
         pipelined sweep with cp.async instead of bulk-tensor copies;
         step_graph=True runs each step (from the fourth) as one CUDA graph launch
-        with the solver's loops on the device."""
+        with the solver's loops on the device; sweep_zchunk and row_blocks_per_sm
+        are launch shapes (z planes per block of the pipelined sweep, blocks per
+        SM of the row-patch kernels; 0 = the library's choice)."""
         m = {"fp64": capi.SOLVER_FP64, "mixed": capi.SOLVER_MIXED}[mode]
         flags = (0 if graphs else capi.SOLVER_NO_GRAPHS) | \
             (capi.SOLVER_EXTRAPOLATE if extrapolate else 0) | \
             (0 if tma else capi.SOLVER_NO_TMA) | \
             (capi.SOLVER_STEP_GRAPH if step_graph else 0)
         o = capi.SolverOpts(m, max_outer, max_inner, smooth_sweeps, rtol, inner_rtol,
-                            sweep_min_cells, w_from_level, flags)
+                            sweep_min_cells, w_from_level, flags, sweep_zchunk, row_blocks_per_sm)
         capi.check(self.L.wpf_set_solver(self.h, C.byref(o)), "wpf_set_solver")
         self.solver = mode
 

@@ -60,6 +60,40 @@ def test_conv3d_matches_oracle(cin, cout):
     assert rel_l2(got16, want16) < 1e-2
 
 
+# (nx, ny, nz) that route 16-channel inputs to the row-tiled kernel, one per
+# brick width: 128 x 1 (one staged 130-voxel row), 64 x 2, 32 x 4, 16 x 8
+ROW_SHAPES = [(128, 3, 4), (64, 4, 3), (96, 4, 2), (48, 8, 3)]
+
+
+@pytest.mark.parametrize("shape", ROW_SHAPES)
+@pytest.mark.parametrize("cout", [16, 32])
+def test_conv3d_row_tiled_matches_oracle(shape, cout):
+    """The TMA-staged row-tiled convolution of the 16-channel layers: zero
+    padding by the copies' out-of-range fill, every tap a window of the
+    staged halo."""
+    import torch
+    capi, L = _lib()
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + ny + cout)
+    x = N.bf16(rng.standard_normal((nz, ny, nx, 16)))
+    w = N.bf16(rng.standard_normal((cout, 27, 16)) * 0.2)
+    b = rng.standard_normal(cout).astype(np.float32)
+    ref = N.conv3d(x, w, b)
+    dx, dw, db = _dev_bf16(x), _dev_bf16(w), _dev_f32(b)
+    out32 = torch.zeros(nz * ny * nx * cout, dtype=torch.float32, device="cuda")
+    capi.check(L.wpf_conv3d(16, cout, nx, ny, nz, _ptr(dx), _ptr(dw), _ptr(db), 0, None,
+                            _ptr(out32), None), "wpf_conv3d")
+    got = out32.cpu().numpy().reshape(nz, ny, nx, cout)
+    assert rel_l2(got, ref) < 1e-5
+    out16 = torch.zeros(nz * ny * nx * cout, dtype=torch.int16, device="cuda")
+    capi.check(L.wpf_conv3d(16, cout, nx, ny, nz, _ptr(dx), _ptr(dw), _ptr(db), 1,
+                            _ptr(out16), None, None), "wpf_conv3d")
+    got16 = N.from_bits(out16.cpu().numpy().view(np.uint16)).reshape(nz, ny, nx, cout)
+    want16 = N.bf16(np.maximum(ref, 0))
+    assert np.mean(got16 != want16) < 0.01
+    assert rel_l2(got16, want16) < 1e-2
+
+
 @pytest.mark.parametrize("cin,cout", PAIRS)
 def test_conv3d_wgrad_matches_oracle(cin, cout):
     import torch

@@ -269,3 +269,34 @@ def test_level0_rebuilt_incrementally(step_graph):
         for key in SAME:
             assert a[key] == b[key], (n, key, a[key], b[key])
         assert abs(a["relres"] - b["relres"]) <= 1e-9, (n, a["relres"], b["relres"])
+
+
+def test_learned_start_in_the_step_graph():
+    """With a warm-start net attached, each step from the fourth is still one
+    graph launch: features, forward pass and prolongation are captured and the
+    step along the net's correction is decided on the device.  Against the
+    host-driven learned step: every solve converges to the same residual
+    tolerance, the net's start is taken, and the fields agree to the solver
+    tolerance (the two runs may take different starts where a feature's last
+    bit differs, so only the converged answer is compared)."""
+    from conftest import rel_l2
+    from mizuho_edit_gb300 import learned
+    case = _case((32, 32, 32), seed=31)
+    out = {}
+    for graph in (False, True):
+        net = learned.WarmStartNet(16, 16, 16, seed=3)
+        try:
+            with _sim(case, solver="mixed", rtol=1e-8, extrapolate=True, step_graph=graph) as sim:
+                learned.attach(sim, net)
+                st = [sim.step().as_dict() for _ in range(14)]
+                learned.attach(sim, None)
+                out[graph] = (st, sim.download(*FIELDS))
+        finally:
+            net.close()
+    host, dev = out[False][0], out[True][0]
+    assert all(s["converged"] and s["relres"] <= 1e-8 for s in host + dev)
+    assert not any(s["device_resident"] for s in host)
+    assert all(s["device_resident"] == 1 for s in dev[3:])
+    assert any(s["warm_start"] == 2 for s in dev[3:])
+    for k in FIELDS:
+        assert rel_l2(out[True][1][k], out[False][1][k]) < 1e-6, k
