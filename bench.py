@@ -361,6 +361,18 @@ class Arms:
             self.net = None
 
 
+def device_memory(arms):
+    """The library's device allocations for this domain (wpf_device_bytes:
+    fields, solver hierarchies of both precisions, the net's buffers) and the
+    device memory in use in the process now, against the HBM size."""
+    import torch
+    from mizuho_edit_gb300 import capi
+    nb = C.c_int64()
+    capi.check(arms.sim.L.wpf_device_bytes(arms.sim.h, C.byref(nb)), "wpf_device_bytes")
+    free, total = torch.cuda.mem_get_info()
+    return {"library_bytes": int(nb.value), "in_use_bytes": int(total - free), "hbm_bytes": int(total)}
+
+
 def roofline_window(args, arms):
     """The finest-level red-black sweep timed per launch (the step's largest
     HBM-bound share): its kernel class is timed with events around every
@@ -411,8 +423,18 @@ def roofline_window(args, arms):
             "traffic_source": "profiles/k_sweep_async_224.md (ncu, 224^3, scaled by cells)",
             "peak_source": peak_kind, "bytes_per_cell_per_launch": per_cell,
             "launches": cnt, "avg_launch_us": smooth_ms * 1000.0 / max(cnt, 1)}
-    breakdown = ({KC_NAMES[c]: float(kms[c]) / args.steps for c in range(NK)}
-                 if args.breakdown else None)
+    breakdown = None
+    if args.breakdown:
+        breakdown = {KC_NAMES[c]: {"ms_per_step": float(kms[c]) / args.steps,
+                                   "launches_per_step": int(kcnt[c]) / args.steps} for c in range(NK)}
+        # the stencil classes whose algorithmic bytes per launch are fixed: the
+        # finest-level sweep (above) and k_apply_p (z, p_old, cx, cy, cz, diag
+        # read, p and q written: 32 B per cell in FP32)
+        apply_ms = float(kms[5])
+        if apply_ms > 0:
+            breakdown["apply"]["achieved_gbs"] = 32.0 * ncell * int(kcnt[5]) / (apply_ms / 1000.0) / 1e9
+        if achieved:
+            breakdown["smooth_l0"]["achieved_gbs"] = achieved
     return roof, breakdown
 
 
@@ -460,6 +482,7 @@ def run_ours(args):
     ncell = args.n ** 3
     value = head_line["value"]
     roof, breakdown = roofline_window(args, arms)
+    memory = device_memory(arms)
     out = {
         "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head_line["ms_per_step"],
@@ -478,6 +501,7 @@ def run_ours(args):
         "roofline": roof,
         "clocks": head_line.get("clocks"),
         "windows": windows,
+        "device_memory": memory,
     }
     last = windows[-1]
     if "plain_fp64" in last:

@@ -147,10 +147,12 @@ typedef struct wpf_diag {
     double phase_max, phase_min, concent_max, concent_min;   /* over G incl. halo      */
     double pressure_ref;       /* getPressure(ix_ref, iy_ref, iz_ref) (:2151-2166)      */
     double inlet_flux;         /* sum of u_x across the faces ix = 1 | 2, times dx^2    */
-    double phase_max_outlet;   /* max phase over the cells ix = nx-1: breakthrough when
-                                  > 0 (no counterpart in the reference, whose
-                                  showProgress cannot report it under Dirichlet BCs);
-                                  NaN from wpf_reduce_noalloc                          */
+    double phase_max_outlet;   /* max phase over the plane ix = nx - ceil(2 w / dx), the
+                                  closest the dissolved region gets to outlet wells that
+                                  pin phase = -1 on ix = nx: breakthrough when > 0 (no
+                                  counterpart in the reference, whose showProgress cannot
+                                  report it under Dirichlet BCs); NaN from
+                                  wpf_reduce_noalloc                                    */
 } wpf_diag;
 
 /* ---- lifetime ------------------------------------------------------------

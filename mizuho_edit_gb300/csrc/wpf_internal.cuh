@@ -562,6 +562,7 @@ __device__ __forceinline__ void block_add(T v, double* acc) {
 
 // ---- cross-file entry points (implemented in wpf_physics.cu / wpf_solver.cu)
 int phys_permeability(wpf_handle* h, bool materialise);
+int breakthrough_plane(const wpf_params& p);   // ix of the breakthrough plane (wpf_diag)
 int phys_velocity(wpf_handle* h);
 int phys_phase_deriv(wpf_handle* h, double* taumin, int32_t* overshoot);
 int phys_concent_deriv(wpf_handle* h);

@@ -642,6 +642,22 @@ __global__ void k_set_dirichlet(double* __restrict__ pr, const long long* __rest
 }
 
 // ---------------------------------------------------------------------------
+// The plane whose phase maximum signals breakthrough: ix = nx - ceil(2 w / dx)
+// (at least 1).  The outlet wells pin phase = -1 on ix = nx (wPFAW3D.f90:474-483)
+// and the diffuse interface, about 2w wide, cannot cross that pinned plane:
+// once the dissolved region arrives, the phase settles into a steady profile
+// that stays below 0 within ~2w of the outlet (measured at 64^3: -0.70, -0.41,
+// -0.14 on ix = nx-1..nx-3, +0.11 on nx-4).  So the dissolved region reaching
+// ix = nx - 2w/dx is the breakthrough event, where the criterion "phase > 0 on
+// ix = nx - 1" of a free outlet never fires.
+int breakthrough_plane(const wpf_params& p) {
+    const double m = 2.0 * p.epsilon / p.dx;
+    int k = (int)ceil(m - 1e-9);
+    if (k < 1) k = 1;
+    const int ix = p.nx - k;
+    return ix >= 1 ? ix : 1;
+}
+
 // showProgress reductions (:1695, :1756-1810): per-block partials of
 //   S0 = sum(1-phase), S1 = sum(1+phase)  (interior, compensated per thread)
 //   M0 = max r^2 over phase > 0, max/min phase, max/min concent (over G)
@@ -659,7 +675,7 @@ __device__ __forceinline__ void two_sum(double& s, double& c, double v) {
     s = t;
 }
 
-__global__ void k_diag_partial(Grid g, Phys P, int ix_ref, int iy_ref, int iz_ref,
+__global__ void k_diag_partial(Grid g, Phys P, int ix_ref, int iy_ref, int iz_ref, int ix_bt,
                                const double* __restrict__ ph, const double* __restrict__ cc,
                                const double* __restrict__ pr, const double* __restrict__ Tx,
                                DiagPart* __restrict__ out) {
@@ -690,7 +706,7 @@ __global__ void k_diag_partial(Grid g, Phys P, int ix_ref, int iy_ref, int iz_re
                     const double u = -(Tx[n] * ((pr[n + 1] - pr[n]) * P.inv_dx));
                     two_sum(s2, c2, u * dx * dx);
                 }
-                if (i == g.nx - 1) omax = fmax(omax, f);   // breakthrough plane
+                if (i == ix_bt) omax = fmax(omax, f);   // breakthrough plane
             }
         }
     DiagPart r;
@@ -968,8 +984,8 @@ int phys_reduce(wpf_handle* h, wpf_diag* d) {
     }
     DiagPart* parts = reinterpret_cast<DiagPart*>(h->partials);
     WPF_LAUNCH(h, KC_OTHER, k_diag_partial<<<nparts, dim3(32, 8), 0, h->stream>>>(
-        g, h->phys, h->prm.ix_ref, h->prm.iy_ref, h->prm.iz_ref, h->phase, h->concent,
-        h->pressure, h->T[0], parts));
+        g, h->phys, h->prm.ix_ref, h->prm.iy_ref, h->prm.iz_ref, breakthrough_plane(h->prm), h->phase,
+        h->concent, h->pressure, h->T[0], parts));
     WPF_LAUNCH(h, KC_OTHER, k_diag_final<<<1, 32, 0, h->stream>>>(parts, nparts, h->dsc + S_SUM0));
     WPF_CUDA(cudaGetLastError());
     WPF_CUDA(cudaMemcpyAsync(h->hsc + S_SUM0, h->dsc + S_SUM0, 9 * sizeof(double),

@@ -232,6 +232,20 @@ class OracleSim:
         self.evolveConcent(self.dtime)
         return info
 
+    def breakthrough_plane(self) -> int:
+        """ix of the plane whose phase maximum signals breakthrough: nx -
+        ceil(2 w / dx), at least 1 (outlet wells pin phase = -1 on ix = nx and
+        the interface, ~2w wide, cannot cross the pinned plane)."""
+        p = self.params
+        k = max(1, int(np.ceil(2.0 * p.epsilon / p.dx - 1e-9)))
+        return max(1, p.nx - k)
+
+    def inlet_flux(self) -> float:
+        """Q_in = sum of u_x over the faces between ix = 1 and 2, times dx^2
+        (the velocity of the last calcVelocity)."""
+        p = self.params
+        return float(self.velocity[0, 1, 1:-1, 1:-1].sum()) * p.dx * p.dx
+
     def diagnostics(self) -> dict:
         d = Diag()
         lib().orc_diagnostics(C.byref(self._st), C.byref(d))
