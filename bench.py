@@ -237,8 +237,9 @@ def config_of(args, world):
             "spinup_form": "extrapolated FP32-refined start, one graph launch per step",
             "multigrid": {"w_cycle_from_level": args.w_from, "sweeps_per_side": args.nu,
                           "pipelined_sweep_min_cells": args.sweep_min or (1 << 23)},
-            "step": ("one CUDA graph launch per step" if not args.no_step_graph else "host-driven")
-                    + ("; the learned arm is host-driven" if arm == "learned" else ""),
+            "step": "one CUDA graph launch per step" if not args.no_step_graph else "host-driven",
+            "learned_correction": "evaluated in the step graph (an IF node) when the extrapolated "
+                                  "start misses the 1e-8 tolerance by at most 4x",
             "l2_policy": "inputs larger than L2 (~3.5 GB of fields and solver levels per step)",
             "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
 

@@ -166,7 +166,7 @@ __global__ void k_step_begin(StepCtl* c, double* dsc, double dt_c, double dt_a) 
         c->wb = (float)(-q / h2);
     }
     c->bnorm = c->relres = c->relres0 = c->r0 = c->tol = 0.0;
-    c->pass = c->outer = c->inner = c->it = c->need_pcg = c->accept = c->used = c->pcgs = 0;
+    c->pass = c->outer = c->inner = c->it = c->need_pcg = c->accept = c->used = c->pcgs = c->net_runs = 0;
     c->alpha = 0.f;
     c->status = WPF_ERR_NOT_CONVERGED;
     for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;   // RR64 BB64 RR0WS RW WW
@@ -324,7 +324,8 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     h->rkeep_ok = h->rkeep && h->opts.mode == WPF_SOLVER_MIXED && c.status != WPF_ERR_NONFINITE;
     h->l0_inc_ok = h->l0mark != nullptr;   // the step rebuilt the level-0 operator
     h->l0_mode = h->opts.mode;
-    const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter;
+    const long long launches = n.fixed + (long long)c.pass * n.per_pass + (long long)c.inner * n.per_iter +
+                               (long long)c.net_runs * n.per_net;
     h->nlaunch += launches;
     int rc = c.status;
     if (h->ws_net && ws_enabled(h) && rc != WPF_ERR_CUDA) {   // the net's kernels' bounded waits

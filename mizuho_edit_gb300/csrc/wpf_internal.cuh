@@ -12,6 +12,7 @@
 
 #include <cuda.h>   // CUtensorMap
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -124,7 +125,7 @@ struct StepCtl {
     int used;                // 1 start used, -1 rejected, 0 not tried
     int status;              // WPF_OK / WPF_ERR_NOT_CONVERGED / WPF_ERR_NONFINITE
     int pcgs;                // PCG runs
-    int pad;
+    int net_runs;            // the learned correction was evaluated this step (0 / 1)
 };
 
 // Builds a CUDA graph from stream-captured segments and conditional nodes.
@@ -154,8 +155,17 @@ constexpr int BRICK_X = 32, BRICK_Y = 4, BRICK_Z = 2;   // fused-update bricks (
 // Kernels launched per step by a captured device-resident step:
 //   fixed + passes * per_pass + iterations * per_iter.
 struct StepCounts {
-    long long fixed = 0, per_pass = 0, per_iter = 0;
+    long long fixed = 0, per_pass = 0, per_iter = 0, per_net = 0;
 };
+
+// The learned correction is tried only when the extrapolated start misses the
+// tolerance by at most this factor: there a small reduction of the start's
+// residual can save a refinement pass; further out the PCG runs anyway.
+constexpr double NET_WINDOW = 4.0;
+__host__ __device__ inline bool net_gate(double rr_ext, double bb, double rtol) {
+    const double rel = bb > 0.0 ? sqrt(rr_ext / bb) : sqrt(rr_ext);
+    return rel > rtol && rel <= NET_WINDOW * rtol;
+}
 
 template <typename R>
 struct Hierarchy {
@@ -237,6 +247,8 @@ struct wpf_handle {
     float* ws_e[2];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output)
     uint16_t* ws_in;         // net input (bf16, net grid, 16 channels)
     float* ws_out;           // net output channel 0 (net grid)
+    float* ws_klog;          // net input channel 0, normalised log K_rock (net grid; K_rock is
+                             // fixed between uploads, so it is made once)
     bool ws_klog_ready;      // S_KLOG0/1 hold the statistics of log K_rock
     // asynchronous output snapshots: FP32 device staging, side stream, events
     float* snap;

@@ -553,39 +553,63 @@ __global__ void k_bias_grad(const bf16_t* __restrict__ gy, int nvox, int cout, f
 
 // ---- elementwise pieces of the U-Net ----------------------------------------------
 // out = 2x2x2 mean of in (dims of in: nx, ny, nz, even)
-__global__ void k_pool2(const bf16_t* __restrict__ in, bf16_t* __restrict__ out, int nx, int ny, int nz,
-                        int C) {
-    const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-    const long long n = (long long)hx * hy * hz * C;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-         q += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(q % C);
-        long long V = q / C;
-        const int X = (int)(V % hx);
-        V /= hx;
-        const int Y = (int)(V % hy), Z = (int)(V / hy);
-        float s = 0.f;
-        for (int k = 0; k < 2; ++k)
-            for (int j = 0; j < 2; ++j)
-                for (int i = 0; i < 2; ++i)
-                    s += bf2f(in[((((long long)(2 * Z + k) * ny + 2 * Y + j) * nx) + 2 * X + i) * C + c]);
-        out[q] = f2bf(0.125f * s);
+// One thread per (coarse voxel, 8-channel chunk): 16-byte loads and stores.
+// Per channel the same sum in the same order as the element-wise form.
+__device__ __forceinline__ void unpack8(const uint4 q, float* f) {
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        f[2 * i] = bf2f((bf16_t)(w[i] & 0xFFFFu));
+        f[2 * i + 1] = bf2f((bf16_t)(w[i] >> 16));
     }
 }
 
-// out = up2(low) + skip (dims of out / skip: nx, ny, nz)
-__global__ void k_up2_add(const bf16_t* __restrict__ low, const bf16_t* __restrict__ skip,
-                          bf16_t* __restrict__ out, int nx, int ny, int nz, int C) {
-    const long long n = (long long)nx * ny * nz * C;
+__global__ void k_pool2(const bf16_t* __restrict__ in, bf16_t* __restrict__ out, int nx, int ny, int nz,
+                        int C) {
+    const int hx = nx / 2, hy = ny / 2, hz = nz / 2, C8 = C / 8;
+    const long long n = (long long)hx * hy * hz * C8;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(q % C);
-        long long v = q / C;
+        const int c8 = (int)(q % C8);
+        long long V = q / C8;
+        const int X = (int)(V % hx);
+        V /= hx;
+        const int Y = (int)(V % hy), Z = (int)(V / hy);
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < 2; ++k)
+            for (int j = 0; j < 2; ++j)
+                for (int i = 0; i < 2; ++i) {
+                    const uint4 v = reinterpret_cast<const uint4*>(
+                        in + ((((long long)(2 * Z + k) * ny + 2 * Y + j) * nx) + 2 * X + i) * C)[c8];
+                    float f[8];
+                    unpack8(v, f);
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) s[e] += f[e];
+                }
+        reinterpret_cast<uint4*>(out)[q] =
+            make_uint4(pack2(0.125f * s[0], 0.125f * s[1]), pack2(0.125f * s[2], 0.125f * s[3]),
+                       pack2(0.125f * s[4], 0.125f * s[5]), pack2(0.125f * s[6], 0.125f * s[7]));
+    }
+}
+
+// out = up2(low) + skip (dims of out / skip: nx, ny, nz); per (voxel, chunk)
+__global__ void k_up2_add(const bf16_t* __restrict__ low, const bf16_t* __restrict__ skip,
+                          bf16_t* __restrict__ out, int nx, int ny, int nz, int C) {
+    const int C8 = C / 8;
+    const long long n = (long long)nx * ny * nz * C8;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int c8 = (int)(q % C8);
+        long long v = q / C8;
         const int x = (int)(v % nx);
         v /= nx;
         const int y = (int)(v % ny), z = (int)(v / ny);
-        const long long P = (((long long)(z / 2) * (ny / 2) + y / 2) * (nx / 2) + x / 2) * C + c;
-        out[q] = f2bf(bf2f(low[P]) + bf2f(skip[q]));
+        const long long P = (((long long)(z / 2) * (ny / 2) + y / 2) * (nx / 2) + x / 2) * C8 + c8;
+        float a[8], b[8];
+        unpack8(reinterpret_cast<const uint4*>(low)[P], a);
+        unpack8(reinterpret_cast<const uint4*>(skip)[q], b);
+        reinterpret_cast<uint4*>(out)[q] = make_uint4(pack2(a[0] + b[0], a[1] + b[1]), pack2(a[2] + b[2], a[3] + b[3]),
+                                                      pack2(a[4] + b[4], a[5] + b[5]), pack2(a[6] + b[6], a[7] + b[7]));
     }
 }
 
@@ -877,18 +901,18 @@ int forward(wpf_net* n, const bf16_t* x, cudaStream_t s) {
     auto B = [&](int l) { return n->p + n->L[l].boff; };
     // encoder
     if ((rc = conv(n, 0, x, n->L[0].w16, 16, 16, true, n->y[0], nullptr, B(0), s))) return rc;
-    k_pool2<<<ew_grid(n->nvox[1] * 16), 256, 0, s>>>(n->y[0], n->p0, n->nx[0], n->ny[0], n->nz[0], 16);
+    k_pool2<<<ew_grid(n->nvox[1] * 16 / 8), 256, 0, s>>>(n->y[0], n->p0, n->nx[0], n->ny[0], n->nz[0], 16);
     if ((rc = conv(n, 1, n->p0, n->L[1].w16, 16, 32, true, n->y[1], nullptr, B(1), s))) return rc;
-    k_pool2<<<ew_grid(n->nvox[2] * 32), 256, 0, s>>>(n->y[1], n->p1, n->nx[1], n->ny[1], n->nz[1], 32);
+    k_pool2<<<ew_grid(n->nvox[2] * 32 / 8), 256, 0, s>>>(n->y[1], n->p1, n->nx[1], n->ny[1], n->nz[1], 32);
     if ((rc = conv(n, 2, n->p1, n->L[2].w16, 32, 64, true, n->y[2], nullptr, B(2), s))) return rc;
-    k_pool2<<<ew_grid(n->nvox[3] * 64), 256, 0, s>>>(n->y[2], n->p2, n->nx[2], n->ny[2], n->nz[2], 64);
+    k_pool2<<<ew_grid(n->nvox[3] * 64 / 8), 256, 0, s>>>(n->y[2], n->p2, n->nx[2], n->ny[2], n->nz[2], 64);
     if ((rc = conv(n, 3, n->p2, n->L[3].w16, 64, 64, true, n->y[3], nullptr, B(3), s))) return rc;
     // decoder
-    k_up2_add<<<ew_grid(n->nvox[2] * 64), 256, 0, s>>>(n->y[3], n->y[2], n->s2, n->nx[2], n->ny[2], n->nz[2], 64);
+    k_up2_add<<<ew_grid(n->nvox[2] * 64 / 8), 256, 0, s>>>(n->y[3], n->y[2], n->s2, n->nx[2], n->ny[2], n->nz[2], 64);
     if ((rc = conv(n, 4, n->s2, n->L[4].w16, 64, 32, true, n->y[4], nullptr, B(4), s))) return rc;
-    k_up2_add<<<ew_grid(n->nvox[1] * 32), 256, 0, s>>>(n->y[4], n->y[1], n->s1, n->nx[1], n->ny[1], n->nz[1], 32);
+    k_up2_add<<<ew_grid(n->nvox[1] * 32 / 8), 256, 0, s>>>(n->y[4], n->y[1], n->s1, n->nx[1], n->ny[1], n->nz[1], 32);
     if ((rc = conv(n, 5, n->s1, n->L[5].w16, 32, 16, true, n->y[5], nullptr, B(5), s))) return rc;
-    k_up2_add<<<ew_grid(n->nvox[0] * 16), 256, 0, s>>>(n->y[5], n->y[0], n->s0, n->nx[0], n->ny[0], n->nz[0], 16);
+    k_up2_add<<<ew_grid(n->nvox[0] * 16 / 8), 256, 0, s>>>(n->y[5], n->y[0], n->s0, n->nx[0], n->ny[0], n->nz[0], 16);
     if ((rc = conv(n, 6, n->s0, n->L[6].w16, 16, 16, false, nullptr, n->out32, B(6), s))) return rc;
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
@@ -1187,14 +1211,32 @@ __device__ __forceinline__ double ws_scale_q(const Grid& g, const double* dsc) {
 
 // Net input: 2x2x2 means of (log K_rock - mean)/sd, phase, pressure, d1/s,
 // (d1 - d2)/q, (phase - phase_prev)/s_phi; channels 6..15 zero.
-__global__ void k_ws_features(Grid g, int nxn, int nyn, int nzn, const double* __restrict__ kr,
+// Channel 0 of the net input, 2x2x2 means of (log K_rock - mean) / sd: K_rock
+// only changes with an upload, so this FP64 log pass runs once, not per solve.
+__global__ void k_ws_klog_feature(Grid g, int nxn, int nyn, int nzn, const double* __restrict__ kr,
+                                  const double* __restrict__ dsc, float* __restrict__ out) {
+    const double N = (double)g.nx * g.ny * g.nz;
+    const double km = dsc[S_KLOG0] / N;
+    const double ksd = sqrt(fmax(dsc[S_KLOG1] / N - km * km, 1e-12));
+    const long long nv = (long long)nxn * nyn * nzn;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+         v += (long long)gridDim.x * blockDim.x) {
+        const int X = (int)(v % nxn);
+        const long long r = v / nxn;
+        const int Y = (int)(r % nyn), Z = (int)(r / nyn);
+        double f = 0.0;
+        for (int c = 0; c < 8; ++c)
+            f += log(kr[g.at(2 * X + 1 + (c & 1), 2 * Y + 1 + ((c >> 1) & 1), 2 * Z + 1 + (c >> 2))]);
+        out[v] = (float)((f / 8 - km) / ksd);
+    }
+}
+
+__global__ void k_ws_features(Grid g, int nxn, int nyn, int nzn, const float* __restrict__ klog,
                               const double* __restrict__ ph, const double* __restrict__ prev,
                               const double* __restrict__ pr, const float* __restrict__ d1,
                               const float* __restrict__ d2, const double* __restrict__ dsc,
                               bf16_t* __restrict__ out) {
     const double N = (double)g.nx * g.ny * g.nz;
-    const double km = dsc[S_KLOG0] / N;
-    const double ksd = sqrt(fmax(dsc[S_KLOG1] / N - km * km, 1e-12));
     const double s = ws_scale_s(g, dsc), q = ws_scale_q(g, dsc);
     const double sp = sqrt(dsc[S_DPH2] / N) + 1e-30;
     const long long nv = (long long)nxn * nyn * nzn;
@@ -1206,14 +1248,13 @@ __global__ void k_ws_features(Grid g, int nxn, int nyn, int nzn, const double* _
         double f[6] = {0, 0, 0, 0, 0, 0};
         for (int c = 0; c < 8; ++c) {
             const long long n = g.at(2 * X + 1 + (c & 1), 2 * Y + 1 + ((c >> 1) & 1), 2 * Z + 1 + (c >> 2));
-            f[0] += log(kr[n]);
             f[1] += ph[n];
             f[2] += pr[n];
             f[3] += d1[n];
             f[4] += (double)d1[n] - (double)d2[n];
             f[5] += ph[n] - prev[n];
         }
-        const float ch[6] = {(float)((f[0] / 8 - km) / ksd), (float)(f[1] / 8), (float)(f[2] / 8),
+        const float ch[6] = {klog[v], (float)(f[1] / 8), (float)(f[2] / 8),
                              (float)(f[3] / 8 / s),           (float)(f[4] / 8 / q), (float)(f[5] / 8 / sp)};
         uint4* o = reinterpret_cast<uint4*>(out + v * 16);
         o[0] = make_uint4(pack2(ch[0], ch[1]), pack2(ch[2], ch[3]), pack2(ch[4], ch[5]), 0u);
@@ -1280,16 +1321,33 @@ __global__ void k_ws_target(Grid g, int nxn, int nyn, int nzn, const float* __re
 
 }  // namespace net
 
+// The log K_rock channel of the net input (statistics, then the net-grid
+// means), made when K_rock changed since the last one.
+static int ws_klog_prepare(wpf_handle* h) {
+    const Grid& g = h->g;
+    cudaStream_t s = h->stream;
+    const int nxn = g.nx / 2, nyn = g.ny / 2, nzn = g.nz / 2;
+    const long long nv = (long long)nxn * nyn * nzn;
+    int rc;
+    if (!h->ws_klog && (rc = dev_alloc(h, (void**)&h->ws_klog, sizeof(float) * nv))) return rc;
+    if (!h->ws_klog_ready) {
+        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KLOG0, 0, 2 * sizeof(double), s));
+        WPF_LAUNCH(h, KC_OTHER, net::k_klog_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->krock, h->dsc));
+        WPF_LAUNCH(h, KC_OTHER, net::k_ws_klog_feature<<<net::ew_grid(nv), 256, 0, s>>>(
+            g, nxn, nyn, nzn, h->krock, h->dsc, h->ws_klog));
+        WPF_CUDA(cudaGetLastError());
+        h->ws_klog_ready = true;
+    }
+    return WPF_OK;
+}
+
 // Net input of the coming solve: e_ext (and its scale) for step size hn,
 // then the features.
 static int ws_prepare_features(wpf_handle* h, double hn, uint16_t* in) {
     const Grid& g = h->g;
     cudaStream_t s = h->stream;
-    if (!h->ws_klog_ready) {
-        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KLOG0, 0, 2 * sizeof(double), s));
-        WPF_LAUNCH(h, KC_OTHER, net::k_klog_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->krock, h->dsc));
-        h->ws_klog_ready = true;
-    }
+    int rc0 = ws_klog_prepare(h);
+    if (rc0) return rc0;
     const double keep = h->ws_hn;
     h->ws_hn = hn;
     float a, b;
@@ -1302,7 +1360,7 @@ static int ws_prepare_features(wpf_handle* h, double hn, uint16_t* in) {
     const int nxn = g.nx / 2, nyn = g.ny / 2, nzn = g.nz / 2;
     const long long nv = (long long)nxn * nyn * nzn;
     WPF_LAUNCH(h, KC_OTHER, net::k_ws_features<<<net::ew_grid(nv), 256, 0, s>>>(
-        g, nxn, nyn, nzn, h->krock, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc, in));
+        g, nxn, nyn, nzn, h->ws_klog, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc, in));
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
@@ -1318,15 +1376,11 @@ int ws_net_correction(wpf_handle* h) {
     if (!h->ws_in && (rc = dev_alloc(h, (void**)&h->ws_in, sizeof(uint16_t) * nv * 16))) return rc;
     if (!h->ws_out && (rc = dev_alloc(h, (void**)&h->ws_out, sizeof(float) * nv))) return rc;
     if (!h->ws_e[1] && (rc = dev_alloc(h, (void**)&h->ws_e[1], sizeof(float) * g.total))) return rc;
-    if (!h->ws_klog_ready) {
-        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KLOG0, 0, 2 * sizeof(double), s));
-        WPF_LAUNCH(h, KC_OTHER, net::k_klog_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->krock, h->dsc));
-        h->ws_klog_ready = true;
-    }
+    if ((rc = ws_klog_prepare(h))) return rc;
     WPF_CUDA(cudaMemsetAsync(h->dsc + S_DPH2, 0, sizeof(double), s));
     WPF_LAUNCH(h, KC_OTHER, net::k_dphase_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->phase, h->phase_n, h->dsc));
     WPF_LAUNCH(h, KC_OTHER, net::k_ws_features<<<net::ew_grid(nv), 256, 0, s>>>(
-        g, nxn, nyn, nzn, h->krock, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc,
+        g, nxn, nyn, nzn, h->ws_klog, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc,
         h->ws_in));
     rc = wpf_net_forward(h->ws_net, h->ws_in, h->ws_out, (void*)s);
     if (rc) return rc;
@@ -1348,11 +1402,7 @@ int ws_net_prepare(wpf_handle* h) {
     if (!h->ws_in && (rc = dev_alloc(h, (void**)&h->ws_in, sizeof(uint16_t) * nv * 16))) return rc;
     if (!h->ws_out && (rc = dev_alloc(h, (void**)&h->ws_out, sizeof(float) * nv))) return rc;
     if (!h->ws_e[1] && (rc = dev_alloc(h, (void**)&h->ws_e[1], sizeof(float) * g.total))) return rc;
-    if (!h->ws_klog_ready) {
-        WPF_CUDA(cudaMemsetAsync(h->dsc + S_KLOG0, 0, 2 * sizeof(double), s));
-        WPF_LAUNCH(h, KC_OTHER, net::k_klog_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->krock, h->dsc));
-        h->ws_klog_ready = true;
-    }
+    if ((rc = ws_klog_prepare(h))) return rc;
     if (h->ws_net_warm != h->ws_net) {
         if ((rc = wpf_net_forward(h->ws_net, h->ws_in, h->ws_out, (void*)s))) return rc;
         h->ws_net_warm = h->ws_net;
@@ -1366,11 +1416,11 @@ int ws_net_capture(wpf_handle* h, cudaStream_t s) {
     const Grid& g = h->g;
     const int nxn = g.nx / 2, nyn = g.ny / 2, nzn = g.nz / 2;
     const long long nv = (long long)nxn * nyn * nzn;
-    if (!h->ws_in || !h->ws_out || !h->ws_e[1] || !h->ws_klog_ready) return WPF_ERR_ARG;
+    if (!h->ws_in || !h->ws_out || !h->ws_e[1] || !h->ws_klog || !h->ws_klog_ready) return WPF_ERR_ARG;
     WPF_CUDA(cudaMemsetAsync(h->dsc + S_DPH2, 0, sizeof(double), s));
     WPF_LAUNCH(h, KC_OTHER, net::k_dphase_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->phase, h->phase_n, h->dsc));
     WPF_LAUNCH(h, KC_OTHER, net::k_ws_features<<<net::ew_grid(nv), 256, 0, s>>>(
-        g, nxn, nyn, nzn, h->krock, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc,
+        g, nxn, nyn, nzn, h->ws_klog, h->phase, h->phase_n, h->pressure, h->ws[0], h->ws[1], h->dsc,
         h->ws_in));
     wpf_net* n = h->ws_net;
     int rc = forward(n, h->ws_in, s);

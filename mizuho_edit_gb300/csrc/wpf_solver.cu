@@ -201,9 +201,6 @@ __device__ __forceinline__ R apply_l0(const R* __restrict__ cx, const R* __restr
 // plain FP64 residual.  With rk_in, r0 is read from the kept FP64 residual
 // (the last pass's, corrected for this step's change of T by calcPermeability)
 // instead of being recomputed.
-// With a learned correction e_net: also w = A'e_net, r_ext.w into S_RW and
-// w.w into S_WW, from which the host takes the step alpha = r.w / w.w that
-// minimises ||r_ext - alpha w|| (so the correction never raises the residual).
 template <typename R, bool KEPT>
 __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restrict__ pr,
                                                    const double* __restrict__ Tx,
@@ -216,11 +213,10 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    const R* __restrict__ cz,
                                                    const R* __restrict__ diag,
                                                    const float* __restrict__ e1,
-                                                   const float* __restrict__ e2,
                                                    R* __restrict__ rout, float* __restrict__ dnew,
                                                    double* dsc, const double* __restrict__ rk_in = nullptr) {
-    double rr1 = 0.0, rr0 = 0.0, bb = 0.0, rw = 0.0, ww = 0.0;
-    R rr1r = 0, rwr = 0, wwr = 0;   // the same sums in R (with D)
+    double rr1 = 0.0, rr0 = 0.0, bb = 0.0;
+    R rr1r = 0;   // the same sum in R (with D)
     float rr0f = 0.f;               // ||r(p)||^2 in FP32 on the kept path (only the fallback test reads it)
     const long long sy = g.P, sz = g.S;
     ROW_LOOP(g) {
@@ -269,18 +265,8 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                 const R r1r = from_f64<R>(r0) - apply_l0(cx, cy, cz, diag, e1, n, sy, sz);
                 rout[n] = r1r;
                 rr1r += r1r * r1r;
-                if (e2) {
-                    const R w = apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
-                    rwr += r1r * w;
-                    wwr += w * w;
-                }
             } else {
                 r1 = r0 - to_f64<R>(apply_l0(cx, cy, cz, diag, e1, n, sy, sz));
-                if (e2) {
-                    const double w = to_f64<R>(apply_l0(cx, cy, cz, diag, e2, n, sy, sz));
-                    rw += r1 * w;
-                    ww += w * w;
-                }
             }
         }
         if (!D || (f & F_DIR)) {
@@ -297,15 +283,9 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
     }
     rr1 += (double)rr1r;
     rr0 += (double)rr0f;
-    rw += (double)rwr;
-    ww += (double)wwr;
     block_add(rr1, dsc + S_RR64);
     block_add(rr0, dsc + S_RR0WS);
     block_add(bb, dsc + S_BB64);
-    if (e2) {
-        block_add(rw, dsc + S_RW);
-        block_add(ww, dsc + S_WW);
-    }
 }
 
 // Accept the learned correction with step alpha: r -= alpha A'e_net,
@@ -322,6 +302,28 @@ __global__ void __launch_bounds__(RB) k_ws_take_net(Grid g, const R* __restrict_
         dnew[n] += alpha * e2[n];
         if (!(fl[n] & F_DIR)) r[n] -= (R)alpha * apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
     }
+}
+
+// The learned correction against the extrapolated start's residual: with
+// w = A'e_net, r_ext.w into S_RW and w.w into S_WW (per thread in precision
+// R, across threads in FP64), from which alpha = r.w / w.w, the step that
+// minimises ||r_ext - alpha w||.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_net_dots(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
+                                                 const R* __restrict__ cz, const R* __restrict__ diag,
+                                                 const uint8_t* __restrict__ fl, const float* __restrict__ e2,
+                                                 const R* __restrict__ r, double* dsc) {
+    const long long sy = g.P, sz = g.S;
+    R rw = 0, ww = 0;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        if (fl[n] & F_DIR) continue;
+        const R w = apply_l0(cx, cy, cz, diag, e2, n, sy, sz);
+        rw += r[n] * w;
+        ww += w * w;
+    }
+    block_add((double)rw, dsc + S_RW);
+    block_add((double)ww, dsc + S_WW);
 }
 
 // p += e (e1 [+ alpha e2]: the accepted start, added once, when e1 != null)
@@ -1747,18 +1749,31 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             float wa = 0.f, wb = 0.f;
             ws_coeffs(h, &wa, &wb);
             if ((rc = ws_build_ext(h, wa, wb))) return rc;
-            const bool net = h->ws_net && h->ws_hist >= 2;
-            if (net && (rc = ws_net_correction(h))) return rc;
             const double* rk_in = (rk && h->rkeep_ok) ? rk : nullptr;
             auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
             WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
                 g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx, H.lv[0].cy,
-                H.lv[0].cz, H.lv[0].diag, h->ws_e[0], net ? h->ws_e[1] : nullptr, H.r, dnew, h->dsc, rk_in));
+                H.lv[0].cz, H.lv[0].diag, h->ws_e[0], H.r, dnew, h->dsc, rk_in));
             WPF_CUDA(cudaGetLastError());
             rc = read_slot(h, S_RR64, 5);
             if (rc) return rc;
             double rstart = h->hsc[S_RR64];
-            const double r0 = h->hsc[S_RR0WS], rw = h->hsc[S_RW], ww = h->hsc[S_WW];
+            const double r0 = h->hsc[S_RR0WS];
+            double rw = 0.0, ww = 0.0;
+            // the learned correction, tried when the extrapolation alone misses rtol
+            // by at most NET_WINDOW (there it can save a refinement pass)
+            const bool net = h->ws_net && h->ws_hist >= 2 &&
+                             net_gate(rstart, h->hsc[S_BB64], h->opts.rtol);
+            if (net) {
+                if ((rc = ws_net_correction(h))) return rc;
+                WPF_CUDA(cudaMemsetAsync(h->dsc + S_RW, 0, 2 * sizeof(double), s));
+                WPF_LAUNCH(h, KC_RESID64, k_net_dots<R><<<rb, RB, 0, s>>>(
+                    g, H.lv[0].cx, H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->flags, h->ws_e[1], H.r, h->dsc));
+                WPF_CUDA(cudaGetLastError());
+                if ((rc = read_slot(h, S_RW, 2))) return rc;
+                rw = h->hsc[S_RW];
+                ww = h->hsc[S_WW];
+            }
             // learned correction: the step that minimises the residual along it
             if (net && ww > 0.0 && rw > 0.0 && rw == rw) {
                 alpha = (float)(rw / ww);
@@ -1890,6 +1905,15 @@ __global__ void k_ctl_accept(StepCtl* c, double* dsc) {
         c->used = -1;
         for (int q = 0; q < 5; ++q) dsc[S_RR64 + q] = 0.0;
     }
+}
+
+// Whether the learned correction is evaluated this step (net_gate on the
+// extrapolated start's residual): the condition of the net's IF node.
+__global__ void k_ctl_net_gate(StepCtl* c, const double* dsc, double rtol, cudaGraphConditionalHandle h_net) {
+    if (threadIdx.x) return;
+    const int run = net_gate(dsc[S_RR64], dsc[S_BB64], rtol) ? 1 : 0;
+    c->net_runs = run;
+    cudaGraphSetConditional(h_net, run);
 }
 
 // The same with a learned correction e_net (S_RW = r_ext.A'e_net, S_WW =
@@ -2052,9 +2076,10 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     // when calcPermeability (captured just before) corrected it for this step
     double* rk = mixed ? h->rkeep : nullptr;
     const double* rk_in = (rk && h->rkeep_ok) ? rk : nullptr;
-    cudaGraphConditionalHandle h_pass, h_it;
+    cudaGraphConditionalHandle h_pass, h_it, h_net = 0;
     int rc;
     if ((rc = gb_handle(b, &h_pass)) || (rc = gb_handle(b, &h_it))) return rc;
+    if (net && (rc = gb_handle(b, &h_net))) return rc;
 
     long long l0 = h->nlaunch;
     if ((rc = phys_set_dirichlet(h))) return rc;
@@ -2071,12 +2096,32 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
             WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
                                                                        d, &c->wa));
         }
-        if (net && (rc = ws_net_capture(h, s))) return rc;   // e_net in ws_e[1]
         auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
         WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
             g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
-            h->ws_e[0], net ? h->ws_e[1] : nullptr, H.r, dnew, d, rk_in));
+            h->ws_e[0], H.r, dnew, d, rk_in));
         if (net) {
+            // the learned correction in an IF node, taken when the extrapolated
+            // start misses rtol by at most NET_WINDOW (k_ctl_net_gate); the
+            // coarse-level branch joins before it
+            if ((rc = gb_join(h))) return rc;
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_net_gate<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h_net));
+            WPF_CUDA(cudaGetLastError());
+            cnt->fixed += h->nlaunch - l0;
+            if ((rc = gb_end(b))) return rc;
+            GraphBuilder nb;
+            if ((rc = gb_cond(b, cudaGraphCondTypeIf, h_net, &nb))) return rc;
+            if ((rc = gb_begin(nb))) return rc;
+            const long long ln = h->nlaunch;
+            if ((rc = ws_net_capture(h, s))) return rc;   // e_net in ws_e[1]
+            WPF_CUDA(cudaMemsetAsync(d + S_RW, 0, 2 * sizeof(double), s));
+            WPF_LAUNCH(h, KC_RESID64, k_net_dots<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags,
+                                                                    h->ws_e[1], H.r, d));
+            WPF_CUDA(cudaGetLastError());
+            cnt->per_net = h->nlaunch - ln;
+            if ((rc = gb_end(nb))) return rc;
+            if ((rc = gb_begin(b))) return rc;
+            l0 = h->nlaunch;
             WPF_LAUNCH(h, KC_OTHER, k_ctl_accept_net<<<1, 32, 0, s>>>(c, d));
             WPF_LAUNCH(h, KC_RESID64, k_ws_take_net_dev<R><<<rb, RB, 0, s>>>(
                 g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags, c, h->ws_e[1], H.r, dnew));
@@ -2093,7 +2138,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     }
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
                                                          mixed, h_pass));
-    if ((rc = gb_join(h))) return rc;
+    if (!net && (rc = gb_join(h))) return rc;   // (with the net it joined before the IF node)
     WPF_CUDA(cudaGetLastError());
     cnt->fixed += h->nlaunch - l0;
     if ((rc = gb_end(b))) return rc;

@@ -142,19 +142,50 @@ def generate(runs: int, n: int, steps: int, spinup: int, seed0: int = 1000, ever
     return pairs
 
 
-def train(net: WarmStartNet, pairs, epochs: int, lr: float, seed: int = 0, log=print):
+def validation_loss(net: WarmStartNet, pairs) -> float:
+    """Mean over pairs of the training loss, mean_v (out_v - target_v)^2,
+    without a parameter update."""
+    import torch
+    if not pairs:
+        return float("nan")
+    out = torch.empty_like(pairs[0][1])
+    tot = 0.0
+    for x, t in pairs:
+        net.forward(x, out)
+        tot += float(((out - t).double() ** 2).mean())
+    return tot / len(pairs)
+
+
+def train(net: WarmStartNet, pairs, epochs: int, lr: float, seed: int = 0, val_frac: float = 0.1,
+          log=print):
+    """Adam over shuffled pairs with a cosine learning-rate schedule; a
+    held-out fraction of the pairs is scored after every epoch and the
+    parameters of the best held-out epoch are kept.  Returns
+    {"train": [mean loss per epoch], "val": [held-out loss per epoch],
+    "best_epoch": e}."""
+    import math
     rng = np.random.default_rng(seed)
-    hist = []
+    idx = rng.permutation(len(pairs))
+    nval = int(len(pairs) * val_frac) if len(pairs) >= 20 else 0
+    val = [pairs[i] for i in idx[:nval]]
+    tr = [pairs[i] for i in idx[nval:]]
+    hist, vhist = [], []
+    best = None
     for ep in range(epochs):
-        order = rng.permutation(len(pairs))
+        lr_ep = lr * 0.5 * (1.0 + math.cos(math.pi * ep / max(epochs, 1)))
         tot = 0.0
-        for q in order:
-            x, t = pairs[q]
-            tot += net.train_step(x, t, lr)
-        hist.append(tot / max(len(pairs), 1))
-        log(f"epoch {ep}: mean loss {hist[-1]:.4e}")
-        lr *= 0.7
-    return hist
+        for q in rng.permutation(len(tr)):
+            x, t = tr[q]
+            tot += net.train_step(x, t, lr_ep)
+        hist.append(tot / max(len(tr), 1))
+        v = validation_loss(net, val) if val else hist[-1]
+        vhist.append(v)
+        if best is None or v < best[0]:
+            best = (v, ep, net.params())
+        log(f"epoch {ep}: lr {lr_ep:.2e} train loss {hist[-1]:.4e} held-out loss {v:.4e}")
+    if best is not None and best[1] != epochs - 1:
+        net.set_params(best[2])
+    return {"train": hist, "val": vhist, "best_epoch": best[1] if best else -1}
 
 
 def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int):
@@ -182,8 +213,8 @@ def main(argv=None):
     t.add_argument("--n", type=int, default=128)
     t.add_argument("--steps", type=int, default=100)
     t.add_argument("--spinup", type=int, default=10)
-    t.add_argument("--epochs", type=int, default=4)
-    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--epochs", type=int, default=12)
+    t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--eval-n", type=int, default=128)
     a = ap.parse_args(argv)
@@ -194,7 +225,9 @@ def main(argv=None):
     hist = train(net, pairs, a.epochs, a.lr, a.seed)
     t2 = time.time()
     meta = {"runs": a.runs, "n": a.n, "steps": a.steps, "spinup": a.spinup, "epochs": a.epochs,
-            "lr": a.lr, "pairs": len(pairs), "loss": hist, "gen_s": t1 - t0, "train_s": t2 - t1}
+            "lr": a.lr, "schedule": "cosine", "pairs": len(pairs), "loss": hist["train"],
+            "val_loss": hist["val"], "best_epoch": hist["best_epoch"], "gen_s": t1 - t0,
+            "train_s": t2 - t1}
     net.save(a.out, meta)
     print(json.dumps(meta))
 

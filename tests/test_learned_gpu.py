@@ -43,18 +43,21 @@ def test_net_start_same_solution():
 
 
 def test_trained_net_gains_over_extrapolation():
-    """Train on pairs the simulator generates (6 seeded 128^3 runs), then on
-    an unseen seed: the network predicts the extrapolation's error (held-out
-    loss well below that of predicting zero, which is the start without it),
-    and its start leaves a residual no larger than the extrapolation's."""
+    """Train on pairs the simulator generates (6 seeded 128^3 runs; cosine
+    schedule, the best held-out epoch kept), then on an unseen seed: the
+    network predicts the extrapolation's error (held-out loss falls during
+    training and ends well below that of predicting zero, which is the start
+    without it), its start leaves a smaller initial residual than the
+    extrapolation's, and the solves take no more PCG iterations."""
     import torch
     learned, make_case, Simulation = _mods()
     pairs = learned.generate(6, 128, 40, 10, seed0=500, log=lambda *a: None)
     held = learned.generate(1, 128, 12, 30, seed0=900, log=lambda *a: None)
     assert len(pairs) >= 200 and len(held) >= 10
     net = learned.WarmStartNet(64, 64, 64, seed=1)
-    hist = learned.train(net, pairs, 4, 2e-3, log=lambda *a: None)
-    assert hist[-1] < hist[0]
+    hist = learned.train(net, pairs, 6, 1e-3, log=lambda *a: None)
+    assert hist["train"][-1] < hist["train"][0]
+    assert min(hist["val"]) < hist["val"][0]
     out = torch.empty(64 ** 3, dtype=torch.float32, device="cuda")
     zero, err = [], []
     for x, t in held:
@@ -70,5 +73,9 @@ def test_trained_net_gains_over_extrapolation():
     # the net's correction enters with the residual-minimising step (kept,
     # code 2, only when that step is positive), so the start never gets worse
     assert all(s[2] in (-1, 1, 2) for s in with_net)
-    assert r_net <= r_base * (1 + 1e-3)
+    assert any(s[2] == 2 for s in with_net)
+    assert r_net < r_base
+    assert sum(s[1] for s in with_net) <= sum(s[1] for s in base)
+    print(f"unseen seed: initial relative residual {r_base:.3e} -> {r_net:.3e} with the net; "
+          f"PCG iterations {sum(s[1] for s in base)} -> {sum(s[1] for s in with_net)}")
     net.close()
