@@ -117,6 +117,12 @@ typedef struct wpf_solver_opts {
  * device.  wpf_ensemble_run then advances all such members in one launch of
  * one graph.  Ignored while kernel timing is on.                           */
 #define WPF_SOLVER_STEP_GRAPH 8
+/* WPF_SOLVER_NET_ALWAYS: with a warm-start net attached (wpf_net.h), evaluate
+ * its correction at every solve with two increments held, not only when the
+ * extrapolated start misses rtol by at most 4x (the default gate, where the
+ * correction can save a refinement pass).  For measuring the net and for
+ * tests; the solves end at the same rtol either way.                       */
+#define WPF_SOLVER_NET_ALWAYS 16
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

@@ -28,6 +28,7 @@ SOLVER_NO_GRAPHS = 1   # wpf_solver_opts.flags bits
 SOLVER_EXTRAPOLATE = 2
 SOLVER_NO_TMA = 4
 SOLVER_STEP_GRAPH = 8
+SOLVER_NET_ALWAYS = 16
 
 
 class WpfError(RuntimeError):

@@ -188,12 +188,14 @@ def train(net: WarmStartNet, pairs, epochs: int, lr: float, seed: int = 0, val_f
     return {"train": hist, "val": vhist, "best_epoch": best[1] if best else -1}
 
 
-def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int):
+def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int, net_always: bool = False):
     """Per-step stats of a run with the extrapolated start, with or without
-    the network: (relres0, inner iterations, warm_start code) per timed step."""
+    the network: (relres0, inner iterations, warm_start code) per timed step.
+    net_always evaluates the net at every solve instead of only where the
+    extrapolation misses the tolerance by at most 4x."""
     out = []
     with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
-                    rtol=1e-8, extrapolate=True) as sim:
+                    rtol=1e-8, extrapolate=True, net_always=net_always) as sim:
         attach(sim, net)
         for _ in range(spinup):
             sim.step()

@@ -131,7 +131,8 @@ def test_breakthrough_64cubed_against_oracle():
     smx, pvmx, _ = _gpu_breakthrough(case, limit, solver="mixed", rtol=1e-8, extrapolate=True,
                                      step_graph=True)
     sln, pvln, kept = _gpu_breakthrough(case, limit, net_weights=learned.DEFAULT_WEIGHTS,
-                                        solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True)
+                                        solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True,
+                                        net_always=True)
     print(f"breakthrough 64^3: oracle step {g['step']} PV {g['pv_injected']:.5f}; FP64 step {s64} "
           f"PV {pv64:.5f}; FP32-refined step {smx} PV {pvmx:.5f}; learned step {sln} PV {pvln:.5f} "
           f"(net start kept {kept} times)")

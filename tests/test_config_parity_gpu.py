@@ -4,7 +4,8 @@ and concentration (relative L2 over the halo arrays).
 
 * 64^3, 200 steps, log-K variance 1, correlation length 4 cells: the plain
   FP64 form, the FP32-refined form (1e-8 Darcy residual, extrapolated start,
-  one graph launch per step) and the same with the learned start.
+  one graph launch per step) and the same with the learned start (its
+  correction evaluated at every solve).
 * 128^3, 500 steps, log-K variance 2, correlation length 8 cells: the plain
   FP64 form against the FP32-refined form, both against the oracle.
 
@@ -38,7 +39,8 @@ def _forms(names):
     forms = {
         "fp64": dict(solver="fp64", rtol=1e-13),
         "mixed": dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True),
-        "learned": dict(solver="mixed", rtol=1e-8, extrapolate=True),
+        # the net evaluated at every solve (not only inside its gate)
+        "learned": dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True, net_always=True),
     }
     return {k: forms[k] for k in names}
 

@@ -67,7 +67,9 @@ def test_trained_net_gains_over_extrapolation():
     assert np.mean(err) < 0.5 * np.mean(zero)
     case = make_case((128, 128, 128), log_var=2.0, corr_len=8.0, seed=901)
     base = learned.evaluate(case, None, 10, 30)
-    with_net = learned.evaluate(case, net, 10, 30)
+    # the net evaluated at every solve (not only inside its gate), so that
+    # every step measures its correction
+    with_net = learned.evaluate(case, net, 10, 30, net_always=True)
     r_base = np.mean([s[0] for s in base])
     r_net = np.mean([s[0] for s in with_net])
     # the net's correction enters with the residual-minimising step (kept,
