@@ -233,13 +233,14 @@ def config_of(args, world):
             "compared_with": f"plain FP64 MG-PCG from the previous pressure on the same state "
                              f"(plain_fp64; W-cycle from level {args.plain_w_from})",
             "timed_steps": f"{w[-1] + args.warmup + 1}..{w[-1] + args.warmup + args.steps} of the run "
-                           f"(spin-up {w[-1]} steps + warm-up {args.warmup} untimed)",
+                           f"(spin-up {w[-1]} steps + warm-up {args.warmup} untimed); every arm is "
+                           f"timed on these steps from the same saved state",
             "spinup_form": "extrapolated FP32-refined start, one graph launch per step",
             "multigrid": {"w_cycle_from_level": args.w_from, "sweeps_per_side": args.nu,
                           "pipelined_sweep_min_cells": args.sweep_min or (1 << 23)},
             "step": "one CUDA graph launch per step" if not args.no_step_graph else "host-driven",
             "learned_correction": "evaluated in the step graph (an IF node) when the extrapolated "
-                                  "start misses the 1e-8 tolerance by at most 4x",
+                                  "start misses the 1e-8 tolerance by at most 1.25x",
             "l2_policy": "inputs larger than L2 (~3.5 GB of fields and solver levels per step)",
             "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
 
@@ -306,6 +307,23 @@ class Arms:
         while self.sim.itime < step:
             self.sim.step()
 
+    def snapshot(self):
+        """The run's state at a window: fields, step number, dt, time, taumin."""
+        sim = self.sim
+        f = sim.download("phase", "concent", "pressure")
+        return (f, sim.itime, sim.dtime, sim.time, sim.taumin)
+
+    def restore(self, snap):
+        """Back to a snapshot, so that every arm is timed on the same steps of
+        the same state (the increment history of the extrapolation is rebuilt
+        by the warm-up steps)."""
+        from mizuho_edit_gb300 import capi
+        f, itime, dtime, tm, taumin = snap
+        sim = self.sim
+        sim.upload(None, f["phase"], f["concent"], f["pressure"])
+        sim.itime, sim.dtime, sim.time, sim.taumin = itime, dtime, tm, taumin
+        capi.check(sim.L.wpf_set_taumin(sim.h, taumin), "wpf_set_taumin")
+
     def time(self, arm, world, clocks=None):
         """(clocks: a running ClockSampler, stopped after the timed steps.)"""
         """W warm-up steps of the arm, then exactly K timed steps between a
@@ -322,12 +340,16 @@ class Arms:
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
+        if clocks:   # the headline region: a profiler run with --profile-from-start off sees it alone
+            torch.cuda.profiler.start()
         sim.L.wpf_launch_count(sim.h, C.byref(n0))
         first = sim.itime + 1
         e0.record(stream)
         stats = [sim.step() for _ in range(args.steps)]
         e1.record(stream)
         torch.cuda.synchronize()
+        if clocks:
+            torch.cuda.profiler.stop()
         sim.L.wpf_launch_count(sim.h, C.byref(n1))
         clk = clocks.stop() if clocks else None
         ms = max_over_ranks(e0.elapsed_time(e1), world)
@@ -464,6 +486,7 @@ def run_ours(args):
     head_line = None
     for wi, w in enumerate(wins):
         arms.advance_to(w)
+        snap = arms.snapshot()
         row = {}
         clocks = None
         if wi == len(wins) - 1:   # sampled over the last window's arms, the headline last
@@ -471,6 +494,7 @@ def run_ours(args):
             clocks.start()
         for arm in arms_list:
             last = wi == len(wins) - 1 and arm == head
+            arms.restore(snap)
             r = arms.time(arm, world, clocks if last else None)
             row[arm] = r
             if last:
@@ -561,7 +585,11 @@ def alt_kwh_pass(args, rank, world, arm_names):
     try:
         for w in windows_of(args):
             arms.advance_to(w)
-            row = {a: arms.time(a, world) for a in arm_names}
+            snap = arms.snapshot()
+            row = {}
+            for a in arm_names:
+                arms.restore(snap)
+                row[a] = arms.time(a, world)
             if "plain_fp64" in row and "extrapolated" in row:
                 row["extrapolated"]["speedup_vs_plain_fp64"] = (row["extrapolated"]["value"] /
                                                                 row["plain_fp64"]["value"])
