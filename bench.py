@@ -43,6 +43,12 @@ KC_NAMES = ["permeability", "resid64", "coefficients", "smooth_l0", "mg_other", 
             "pcg_vec", "fused_update", "other", "bottom"]
 # the timed forms ("arms") of the Darcy solve, all on the same run's state
 ARMS = ("learned", "extrapolated", "plain_fp64")
+# Untimed steps before each arm's W warm-up steps: a step graph bakes in its
+# buffers, the step's ping-pong buffers cycle with period 6 and the first
+# steps after a solver switch or an upload run with transient state, so the
+# first ~8 steps of an arm capture graphs (tens of ms each at 512^3) that the
+# rest of a long run replays.
+GRAPH_WARMUP = 8
 
 
 def parse():
@@ -232,15 +238,17 @@ def config_of(args, world):
             "warm_start": start, "form": arm,
             "compared_with": f"plain FP64 MG-PCG from the previous pressure on the same state "
                              f"(plain_fp64; W-cycle from level {args.plain_w_from})",
-            "timed_steps": f"{w[-1] + args.warmup + 1}..{w[-1] + args.warmup + args.steps} of the run "
-                           f"(spin-up {w[-1]} steps + warm-up {args.warmup} untimed); every arm is "
-                           f"timed on these steps from the same saved state",
+            "timed_steps": f"{w[-1] + GRAPH_WARMUP + args.warmup + 1}.."
+                           f"{w[-1] + GRAPH_WARMUP + args.warmup + args.steps} of the run (spin-up "
+                           f"{w[-1]} steps, then per arm {GRAPH_WARMUP} steps that capture its step "
+                           f"graphs and {args.warmup} warm-up steps, untimed); every arm is timed on "
+                           f"these steps from the same saved state",
             "spinup_form": "extrapolated FP32-refined start, one graph launch per step",
             "multigrid": {"w_cycle_from_level": args.w_from, "sweeps_per_side": args.nu,
                           "pipelined_sweep_min_cells": args.sweep_min or (1 << 23)},
             "step": "one CUDA graph launch per step" if not args.no_step_graph else "host-driven",
             "learned_correction": "evaluated in the step graph (an IF node) when the extrapolated "
-                                  "start misses the 1e-8 tolerance by at most 1.25x",
+                                  "start misses the 1e-8 tolerance by at most 1.02x (the net's measured reach)",
             "l2_policy": "inputs larger than L2 (~3.5 GB of fields and solver levels per step)",
             "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
 
@@ -325,14 +333,14 @@ class Arms:
         capi.check(sim.L.wpf_set_taumin(sim.h, taumin), "wpf_set_taumin")
 
     def time(self, arm, world, clocks=None):
-        """(clocks: a running ClockSampler, stopped after the timed steps.)"""
-        """W warm-up steps of the arm, then exactly K timed steps between a
-        barrier + synchronize and a synchronize, CUDA events on the library's
-        stream; max over ranks."""
+        """GRAPH_WARMUP steps that capture the arm's step graphs, W warm-up
+        steps, then exactly K timed steps between a barrier + synchronize and
+        a synchronize, CUDA events on the library's stream; max over ranks.
+        clocks: a running ClockSampler, stopped after the timed steps."""
         import torch
         args, sim = self.args, self.sim
         self.set(arm)
-        for _ in range(args.warmup):
+        for _ in range(GRAPH_WARMUP + args.warmup):
             sim.step()
         stream = self.stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -119,7 +119,7 @@ typedef struct wpf_solver_opts {
 #define WPF_SOLVER_STEP_GRAPH 8
 /* WPF_SOLVER_NET_ALWAYS: with a warm-start net attached (wpf_net.h), evaluate
  * its correction at every solve with two increments held, not only when the
- * extrapolated start misses rtol by at most 1.25x (the default gate, where the
+ * extrapolated start misses rtol by at most 1.02x (the default gate, where the
  * correction can save a refinement pass).  For measuring the net and for
  * tests; the solves end at the same rtol either way.                       */
 #define WPF_SOLVER_NET_ALWAYS 16

@@ -161,10 +161,10 @@ struct StepCounts {
 // The learned correction is tried only when the extrapolated start misses the
 // tolerance by at most this factor: there a small reduction of the start's
 // residual can save a refinement pass; further out the PCG runs anyway.  The
-// trained net lowers the start's residual by about 1 % on unseen seeds
-// (9.14e-8 -> 9.07e-8 mean over ten 128^3 steps), so a start more than a
-// quarter above the tolerance is out of its reach.
-constexpr double NET_WINDOW = 1.25;
+// trained net lowers the start's residual by 0.7 % on unseen seeds (9.14e-8 ->
+// 9.07e-8, mean over ten 128^3 steps), so a start more than 2 % above the
+// tolerance is out of its reach.
+constexpr double NET_WINDOW = 1.02;
 __host__ __device__ inline bool net_gate(double rr_ext, double bb, double rtol) {
     const double rel = bb > 0.0 ? sqrt(rr_ext / bb) : sqrt(rr_ext);
     return rel > rtol && rel <= NET_WINDOW * rtol;

@@ -192,7 +192,7 @@ def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int, net_always
     """Per-step stats of a run with the extrapolated start, with or without
     the network: (relres0, inner iterations, warm_start code) per timed step.
     net_always evaluates the net at every solve instead of only where the
-    extrapolation misses the tolerance by at most 1.25x."""
+    extrapolation misses the tolerance by at most 1.02x."""
     out = []
     with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
                     rtol=1e-8, extrapolate=True, net_always=net_always) as sim:

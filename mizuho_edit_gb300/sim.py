@@ -117,7 +117,7 @@ class Simulation:
         are launch shapes (z planes per block of the pipelined sweep, blocks per
         SM of the row-patch kernels; 0 = the library's choice); net_always
         evaluates an attached net's correction at every solve instead of only
-        when the extrapolated start misses rtol by at most 1.25x."""
+        when the extrapolated start misses rtol by at most 1.02x."""
         m = {"fp64": capi.SOLVER_FP64, "mixed": capi.SOLVER_MIXED}[mode]
         flags = (0 if graphs else capi.SOLVER_NO_GRAPHS) | \
             (capi.SOLVER_EXTRAPOLATE if extrapolate else 0) | \
