@@ -14,6 +14,7 @@ network), so the network changes iteration counts, never the answer.
 PyTorch only holds device memory here; every kernel is the library's.
 
     python -m mizuho_edit_gb300.learned train --out weights.npz [--runs 20 --n 128 ...]
+    python -m mizuho_edit_gb300.learned time --grid 128      # forward-pass time
 """
 from __future__ import annotations
 
@@ -206,6 +207,29 @@ def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int, net_always
     return out
 
 
+def time_forward(m: int, reps: int = 5) -> dict:
+    """Forward pass of a seeded net on an m^3 net grid (the solve at (2m)^3
+    cells), random BF16 input, one untimed pass, then `reps` timed with CUDA
+    events on the default stream."""
+    import torch
+    net = WarmStartNet(m, m, m, seed=1)
+    try:
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn(m ** 3 * 16, device="cuda", generator=gen).to(torch.bfloat16).view(torch.int16)
+        out = torch.empty(m ** 3, dtype=torch.float32, device="cuda")
+        net.forward(x, out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            net.forward(x, out)
+        e1.record()
+        torch.cuda.synchronize()
+        return {"net_grid": m, "forward_ms": e0.elapsed_time(e1) / max(reps, 1)}
+    finally:
+        net.close()
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -219,7 +243,13 @@ def main(argv=None):
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--eval-n", type=int, default=128)
+    f = sub.add_parser("time", help="time the forward pass on an m^3 net grid (random input)")
+    f.add_argument("--grid", type=int, default=128)
+    f.add_argument("--reps", type=int, default=5)
     a = ap.parse_args(argv)
+    if a.cmd == "time":
+        print(json.dumps(time_forward(a.grid, a.reps)))
+        return
     t0 = time.time()
     pairs = generate(a.runs, a.n, a.steps, a.spinup)
     t1 = time.time()
