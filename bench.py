@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--nu", type=int, default=2, help="smoothing sweeps per side of a cycle")
     ap.add_argument("--sweep-min", type=int, default=0,
                     help="cells from which a level uses the pipelined sweep (0 = library default)")
+    ap.add_argument("--sweep-zchunk", type=int, default=0,
+                    help="z planes per block of the pipelined sweep (0 = the wave-filling chunk)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the preconditioner cycle kernel by kernel")
     ap.add_argument("--no-tma", action="store_true",
@@ -107,7 +109,7 @@ def arm_kwargs(args, arm):
     plain = arm == "plain_fp64"
     return dict(mode="fp64" if plain else "mixed", rtol=args.rtol,
                 w_from_level=args.plain_w_from if plain else args.w_from,
-                smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min,
+                smooth_sweeps=args.nu, sweep_min_cells=args.sweep_min, sweep_zchunk=args.sweep_zchunk,
                 graphs=not args.no_graphs, tma=not args.no_tma,
                 step_graph=not args.no_step_graph, extrapolate=not plain)
 
