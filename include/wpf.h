@@ -123,6 +123,14 @@ typedef struct wpf_solver_opts {
  * correction can save a refinement pass).  For measuring the net and for
  * tests; the solves end at the same rtol either way.                       */
 #define WPF_SOLVER_NET_ALWAYS 16
+/* WPF_SOLVER_FP64_UPDATE: in the FP32-refined form (WPF_SOLVER_MIXED), keep
+ * the fused update's concentration rate of concentration-only cells (uniform
+ * phase neighbourhood) in FP64.  By default that form takes it in FP32 from
+ * the FP64 state (pressure differences in FP64; the rate added to the FP64
+ * concentration as c + dt * rate), which removes most of the update's FP64
+ * work once the acid has spread; the plain FP64 form and the per-routine
+ * entry points are always FP64.                                            */
+#define WPF_SOLVER_FP64_UPDATE 32
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

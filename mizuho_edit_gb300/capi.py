@@ -29,6 +29,7 @@ SOLVER_EXTRAPOLATE = 2
 SOLVER_NO_TMA = 4
 SOLVER_STEP_GRAPH = 8
 SOLVER_NET_ALWAYS = 16
+SOLVER_FP64_UPDATE = 32
 
 
 class WpfError(RuntimeError):

@@ -238,6 +238,42 @@ __device__ __forceinline__ double concent_cell(const double* __restrict__ C, lon
     return P.diffusion * lap + P.alpha * dphidt - div;
 }
 
+// dconcentdt of a concentration-only cell (bitwise-uniform phase
+// neighbourhood, so dphase/dt = 0 and the reaction term vanishes) for the
+// FP32-refined form: the pressure differences of the six face velocities are
+// taken in FP64 (they cancel), the rest -- face velocities, the upwind
+// fluxes, the Laplacian in difference form -- in FP32, the conversions on the
+// integer pipe.  The rate enters the FP64 state as c + dt * rate; its FP32
+// rounding (~1e-7 of the step's change) stays far below the form's
+// tolerance.  Folds |u| of the three + faces into umax.
+struct LoConst {
+    float diffusion, inv_dx, inv_dx2;
+};
+__device__ __forceinline__ float concent_rate_lo(const double* __restrict__ C, const double* __restrict__ pr,
+                                                 const double* __restrict__ Tvx, const double* __restrict__ Tvy,
+                                                 const double* __restrict__ Tvz, long long n, long long sy,
+                                                 long long sz, const LoConst& K, unsigned long long& umax) {
+    const double p0 = pr[n];
+    const float uxp = -(f64_to_f32(Tvx[n]) * f64_to_f32(pr[n + 1] - p0));
+    const float uxm = -(f64_to_f32(Tvx[n - 1]) * f64_to_f32(p0 - pr[n - 1]));
+    const float uyp = -(f64_to_f32(Tvy[n]) * f64_to_f32(pr[n + sy] - p0));
+    const float uym = -(f64_to_f32(Tvy[n - sy]) * f64_to_f32(p0 - pr[n - sy]));
+    const float uzp = -(f64_to_f32(Tvz[n]) * f64_to_f32(pr[n + sz] - p0));
+    const float uzm = -(f64_to_f32(Tvz[n - sz]) * f64_to_f32(p0 - pr[n - sz]));
+    const float c0 = f64_to_f32(C[n]);
+    const float ce = f64_to_f32(C[n + 1]), cw = f64_to_f32(C[n - 1]), cn = f64_to_f32(C[n + sy]);
+    const float cs = f64_to_f32(C[n - sy]), ct = f64_to_f32(C[n + sz]), cb = f64_to_f32(C[n - sz]);
+    const float lap = (((ce - c0) + (cw - c0)) + ((cn - c0) + (cs - c0)) + ((ct - c0) + (cb - c0))) * K.inv_dx2;
+    const float fxp = uxp * (uxp > 0.f ? c0 : ce), fxm = uxm * (uxm > 0.f ? cw : c0);   // strict > 0, :1593
+    const float fyp = uyp * (uyp > 0.f ? c0 : cn), fym = uym * (uym > 0.f ? cs : c0);
+    const float fzp = uzp * (uzp > 0.f ? c0 : ct), fzm = uzm * (uzm > 0.f ? cb : c0);
+    const float div = ((fxp - fxm) + (fyp - fym) + (fzp - fzm)) * K.inv_dx;
+    max_abs_bits(umax, f32_to_f64(uxp));
+    max_abs_bits(umax, f32_to_f64(uyp));
+    max_abs_bits(umax, f32_to_f64(uzp));
+    return K.diffusion * lap - div;
+}
+
 // kmax: the largest kxx of the block's cells (0 if none), so that the block's
 // smallest relaxation time is tau_num / kmax
 __device__ __forceinline__ void flush_step_reductions(double kmax, double tau_num, int over, double umax,
@@ -563,6 +599,9 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
         atomicMin(reinterpret_cast<unsigned long long*>(dsc + S_TAUMIN_KEY), dkey(tau0));
 }
 
+// LOWC: the concentration-only cells take concent_rate_lo (the FP32-refined
+// form); the plain FP64 form keeps every rate in FP64.
+template <bool LOWC>
 __global__ void __launch_bounds__(RB) k_update_active(Grid g, const Phys* __restrict__ Pp,
                                                       const double* __restrict__ ph,
                                                       const double* __restrict__ cc,
@@ -578,6 +617,8 @@ __global__ void __launch_bounds__(RB) k_update_active(Grid g, const Phys* __rest
                                                       double* dsc, const double* dtp = nullptr) {
     if (dtp) dt = *dtp;   // device-resident step: dt from the device dt law
     const Phys P = *Pp;
+    LoConst K{};
+    if (LOWC) K = LoConst{f64_to_f32(P.diffusion), f64_to_f32(P.inv_dx), f64_to_f32(P.inv_dx2)};
     double kmax = 0.0;
     unsigned long long umax = 0;   // bits of the largest |u|
     int overs = 0;
@@ -616,6 +657,7 @@ __global__ void __launch_bounds__(RB) k_update_active(Grid g, const Phys* __rest
         double crate;
         if (well) crate = 0.0;
         else if (concent_zero(cc, n, sy, sz)) crate = P.alpha * rate;
+        else if (LOWC && uni) crate = f32_to_f64(concent_rate_lo(cc, pr, Tvx, Tvy, Tvz, n, sy, sz, K, umax));
         else crate = concent_cell(cc, n, sy, sz, vel(), rate, P);
         const double phn = ph[n] + rate * dt;
         const double ccn = conc + crate * dt;
@@ -894,6 +936,12 @@ void update_advance_bricks(wpf_handle* h) {
     h->bact_ok = true;
 }
 
+// The FP32-refined form takes the concentration-only rates in FP32 unless
+// WPF_SOLVER_FP64_UPDATE keeps them in FP64; the plain form always does.
+static bool low_precision_rates(const wpf_handle* h) {
+    return h->opts.mode == WPF_SOLVER_MIXED && !(h->opts.flags & WPF_SOLVER_FP64_UPDATE);
+}
+
 int phys_fused_update(wpf_handle* h, double dtime, double* taumin, int32_t* overshoot,
                       double* umax) {
     const Grid& g = h->g;
@@ -906,9 +954,10 @@ int phys_fused_update(wpf_handle* h, double dtime, double* taumin, int32_t* over
     WPF_LAUNCH(h, KC_FUSED, k_update_split<<<split_blocks(h), RB, 0, h->stream>>>(
         g, h->phase, h->concent, h->flags, h->phase_n, h->concent_n, h->work, nwork, h->phys.tau0,
         h->dsc, h->bact_ok ? h->bact[0] : nullptr, h->bact[1]));
-    WPF_LAUNCH(h, KC_FUSED, k_update_active<<<(unsigned)h->nsm * 2, RB, 0, h->stream>>>(
+    auto* upd = low_precision_rates(h) ? k_update_active<true> : k_update_active<false>;
+    WPF_LAUNCH(h, KC_FUSED, upd<<<(unsigned)h->nsm * 2, RB, 0, h->stream>>>(
         g, h->dphys, h->phase, h->concent, h->pressure, h->Tv[0], h->Tv[1], h->Tv[2], h->flags,
-        h->work, nwork, h->phase_n, h->concent_n, dtime, h->dsc));
+        h->work, nwork, h->phase_n, h->concent_n, dtime, h->dsc, nullptr));
     WPF_CUDA(cudaGetLastError());
     WPF_CUDA(cudaEventRecord(h->ev[3], h->stream));
     double* t = h->phase; h->phase = h->phase_n; h->phase_n = t;
@@ -956,7 +1005,8 @@ int phys_capture_update(wpf_handle* h, const double* dtp, cudaStream_t s, bool s
     int* nwork = reinterpret_cast<int*>(h->dsc + S_NWORK);
     int rc;
     if (!split_done && (rc = phys_capture_split(h, s))) return rc;
-    WPF_LAUNCH(h, KC_FUSED, k_update_active<<<(unsigned)h->nsm * 2, RB, 0, s>>>(
+    auto* upd = low_precision_rates(h) ? k_update_active<true> : k_update_active<false>;
+    WPF_LAUNCH(h, KC_FUSED, upd<<<(unsigned)h->nsm * 2, RB, 0, s>>>(
         g, h->dphys, h->phase, h->concent, h->pressure, h->Tv[0], h->Tv[1], h->Tv[2], h->flags,
         h->work, nwork, h->phase_n, h->concent_n, 0.0, h->dsc, dtp));
     WPF_CUDA(cudaGetLastError());
