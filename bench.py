@@ -373,6 +373,7 @@ class Arms:
                "relres_max": max(s.relres for s in stats),
                "fused_update_ms": statistics.mean(s.update_ms for s in stats),
                "update_active_fraction": statistics.mean(s.active_cells for s in stats) / ncell,
+               "update_interface_fraction": statistics.mean(s.interface_cells for s in stats) / ncell,
                "max_courant": max(s.max_courant for s in stats),
                "gpu_launches": int(n1.value - n0.value)}
         if arm != "plain_fp64":
@@ -532,6 +533,7 @@ def run_ours(args):
         "relres0_mean": head_line["relres0_mean"],
         "fused_update_ms": head_line["fused_update_ms"],
         "update_active_fraction": head_line["update_active_fraction"],
+        "update_interface_fraction": head_line["update_interface_fraction"],
         "gpu_launches": head_line["gpu_launches"],
         "roofline": roof,
         "clocks": head_line.get("clocks"),

@@ -151,6 +151,8 @@ typedef struct wpf_step_stats {
     int32_t active_cells;      /* cells the fused update evaluated in FP64 (interface and
                                   concentration work lists; the rest were copies)       */
     int32_t device_resident;   /* 1: the step ran as one graph launch (STEP_GRAPH)      */
+    int32_t interface_cells;   /* of active_cells, those on the interface list (the
+                                  phase-field path; the rest are concentration-only)    */
 } wpf_step_stats;
 
 /* showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux. */

@@ -99,6 +99,7 @@ module wpf_gb300
       real(c_double) :: relres0
       integer(c_int32_t) :: active_cells
       integer(c_int32_t) :: device_resident
+      integer(c_int32_t) :: interface_cells
    end type wpf_step_stats
 
    ! showProgress reductions (wPFAW3D.f90:1695, 1756-1810) + inlet flux

@@ -66,7 +66,8 @@ class StepStats(C.Structure):
                 ("taumin", C.c_double), ("dtime", C.c_double), ("max_courant", C.c_double),
                 ("solve_ms", C.c_double), ("update_ms", C.c_double),
                 ("kernel_launches", C.c_int32), ("warm_start", C.c_int32),
-                ("relres0", C.c_double), ("active_cells", C.c_int32), ("device_resident", C.c_int32)]
+                ("relres0", C.c_double), ("active_cells", C.c_int32), ("device_resident", C.c_int32),
+                ("interface_cells", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -700,6 +700,7 @@ int wpf_step(wpf_handle* h, int32_t itime, double* dtime_inout, wpf_step_stats* 
     s->max_courant = umax * dt / p.dx;
     s->kernel_launches = (int32_t)(h->nlaunch - l0);
     s->active_cells = (int32_t)h->last_active;
+    s->interface_cells = (int32_t)h->last_interface;
     s->device_resident = 0;
     *dtime_inout = dt;
     return srs;

@@ -297,6 +297,7 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     const double taumin = dkey_inv(key);
     h->taumin_last = taumin;
     h->last_active = nw[0] + nw[1];
+    h->last_interface = nw[0];
     h->ws_hn = c.dt;
     h->ws_used = c.used;
     if (c.used < 0) ++h->ws_fallbacks;
@@ -356,6 +357,7 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
         st->max_courant = umax * c.dt / h->prm.dx;
         st->kernel_launches = (int32_t)launches;
         st->active_cells = (int32_t)h->last_active;
+        st->interface_cells = (int32_t)h->last_interface;
         st->device_resident = 1;
     }
     cudaGetLastError();

@@ -275,6 +275,7 @@ struct wpf_handle {
     uint8_t* bact[2];
     bool bact_ok;
     int last_active;         // its length in the last step
+    int last_interface;      // of which interface cells
     wpf::Phys* dphys;        // device copy of phys
     long long nlaunch;       // kernels launched on this handle so far
     // per-kernel-class event timers (enabled by wpf_set_kernel_timing)

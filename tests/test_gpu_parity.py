@@ -400,3 +400,60 @@ def test_mixed_form_fp32_concentration_rates(oracle_mod):
         assert rel_l2(fa[k], getattr(ref, k)) < 1e-6, k
         assert rel_l2(fb[k], getattr(ref, k)) < 1e-6, k
         assert rel_l2(fa[k], fb[k]) < 1e-6, k
+
+
+def _front_state(case, axis):
+    """A planar tanh front of width w = 2 normal to `axis` (0: x, 2: z), its
+    tails reaching -1 and 1 to the last bits: the gradient has one nonzero
+    component, down to a few ulp in the tails."""
+    from mizuho_edit_gb300.cases import grf
+    p = case.params
+    shape = (p.nx, p.ny, p.nz)
+    idx = np.indices(shape)[axis].astype(float)
+    ph = np.tanh(-(idx - 0.45 * shape[axis]) / (np.sqrt(2.0) * 2.0))
+    cc = np.clip(0.5 + 0.5 * grf(shape, 3.0, 77), 0, 1)
+    ph[0] = 1.0
+    ph[-1] = -1.0
+    cc[0] = 1.0
+    cc[-1] = 0.0
+    case.phase, case.concent = ph, cc
+    return case
+
+
+@pytest.mark.parametrize("state", ["rough", "front_x", "front_z"])
+def test_mixed_form_fp32_rates_one_step(state):
+    """The FP32-refined form takes the rates of its interface cells (the
+    guard-free path of calcPhaseDeriv) and of its concentration-only cells in
+    FP32, from FP64 differences of the state.  One step against the same step
+    with FP64 rates (WPF_SOLVER_FP64_UPDATE): the pressure solve is the same,
+    so the fields differ only by the rates' precision -- at most 1e-5 of the
+    step's largest change, with the same relaxation time to 1e-6.  The rough
+    state has tanh tails of every size; the fronts have gradients along x only
+    (the FP32 path) and along z only (handed to the FP64 path).
+
+    One step only: past it the two runs differ by ~1e-7, and the model itself
+    amplifies such differences where a gradient lies along z, since W depends
+    on the direction of the vanishing in-plane gradient (theta of :1289): on
+    the z front, differences below 1e-7 after two steps grew to 7e-5 in the
+    third."""
+    _, Simulation = _sim_mod()
+    case = _case((24, 20, 16), seed=21, log_var=2.0, corr_len=4.0)
+    case = _rough_state(case, seed=9) if state == "rough" else _front_state(case, 0 if state == "front_x" else 2)
+    p = case.params
+    kw = dict(solver="mixed", rtol=1e-8)
+    a = Simulation(p, case.permeab_rock, case.phase, case.concent, **kw)
+    b = Simulation(p, case.permeab_rock, case.phase, case.concent, fp64_update=True, **kw)
+    with a, b:
+        f0 = a.download("phase", "concent")
+        sa, sb = a.step(), b.step()
+        fa = a.download("phase", "concent", "pressure")
+        fb = b.download("phase", "concent", "pressure")
+    assert sa.interface_cells > 0 and sa.interface_cells == sb.interface_cells
+    assert sa.taumin == pytest.approx(sb.taumin, rel=1e-6)
+    assert np.array_equal(fa["pressure"], fb["pressure"])
+    for k in ("phase", "concent"):
+        assert np.isfinite(fa[k]).all(), k
+        change = np.abs(fb[k] - f0[k]).max()
+        assert change > 0, k
+        assert np.abs(fa[k] - fb[k]).max() <= 1e-5 * change, k
+        assert np.any(fa[k] != fb[k]), k          # the FP32 path ran
