@@ -642,6 +642,9 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
     const int nbz = (g.nz + BRICK_Z - 1) / BRICK_Z;
     const int nb = nbx * nby * nbz;
     const int lane = threadIdx.x & 31, wy = (threadIdx.x >> 5) & 3, wz = threadIdx.x >> 7;
+    constexpr int SPLIT_WARPS = RB / 32;
+    static_assert(SPLIT_WARPS == BRICK_Y * BRICK_Z, "one warp per brick row");
+    __shared__ int s_cnt[2][SPLIT_WARPS], s_base[2], s_tot[2];
     int any_copy = 0;
     for (int t = blockIdx.x; t < nb; t += gridDim.x) {
         const int bx = t % nbx, r = t / nbx, by = r % nby, bz = r / nby;
@@ -677,24 +680,33 @@ __global__ void __launch_bounds__(RB) k_update_split(Grid g, const double* __res
                 any_copy = 1;
             }
         }
+        // one atomic per list and brick: the two counters are the same two
+        // addresses for every block, and atomics on one address serialise
         const unsigned ma = __ballot_sync(0xffffffffu, !uni);          // interface cells
         const unsigned mb = __ballot_sync(0xffffffffu, uni && !copy);  // concentration-only cells
-        if (ma) {
-            const int leader = __ffs(ma) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(nwork, __popc(ma));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (!uni) work[base + __popc(ma & ((1u << lane) - 1))] = (int)n;
+        const int warp = threadIdx.x >> 5;
+        if (lane == 0) {
+            s_cnt[0][warp] = __popc(ma);
+            s_cnt[1][warp] = __popc(mb);
         }
-        if (mb) {
-            const int leader = __ffs(mb) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(nwork + 1, __popc(mb));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (uni && !copy) work[cap - 1 - (base + __popc(mb & ((1u << lane) - 1)))] = (int)n;
+        __syncthreads();
+        if (threadIdx.x < 2) {
+            int tot = 0;
+            for (int w = 0; w < SPLIT_WARPS; ++w) tot += s_cnt[threadIdx.x][w];
+            s_base[threadIdx.x] = tot ? atomicAdd(nwork + threadIdx.x, tot) : 0;
+            s_tot[threadIdx.x] = tot;
         }
-        const int active = __syncthreads_or(!copy);
-        if (threadIdx.x == 0 && bact_cur) bact_cur[t] = (uint8_t)active;
+        __syncthreads();
+        int offa = s_base[0], offb = s_base[1];
+        for (int w = 0; w < warp; ++w) {
+            offa += s_cnt[0][w];
+            offb += s_cnt[1][w];
+        }
+        const unsigned below = (1u << lane) - 1;
+        if (!uni) work[offa + __popc(ma & below)] = (int)n;
+        if (uni && !copy) work[cap - 1 - (offb + __popc(mb & below))] = (int)n;
+        if (threadIdx.x == 0 && bact_cur) bact_cur[t] = (uint8_t)((s_tot[0] + s_tot[1]) > 0);
+        __syncthreads();   // s_cnt / s_tot are rewritten for the next brick
     }
     if (__syncthreads_or(any_copy) && threadIdx.x == 0)
         atomicMin(reinterpret_cast<unsigned long long*>(dsc + S_TAUMIN_KEY), dkey(tau0));
