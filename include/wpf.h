@@ -124,13 +124,20 @@ typedef struct wpf_solver_opts {
  * tests; the solves end at the same rtol either way.                       */
 #define WPF_SOLVER_NET_ALWAYS 16
 /* WPF_SOLVER_FP64_UPDATE: in the FP32-refined form (WPF_SOLVER_MIXED), keep
- * the fused update's concentration rate of concentration-only cells (uniform
- * phase neighbourhood) in FP64.  By default that form takes it in FP32 from
- * the FP64 state (pressure differences in FP64; the rate added to the FP64
- * concentration as c + dt * rate), which removes most of the update's FP64
- * work once the acid has spread; the plain FP64 form and the per-routine
- * entry points are always FP64.                                            */
+ * the fused update's rates in FP64.  By default that form takes the rates of
+ * its concentration-only cells and of its interface cells on the guard-free
+ * phase path in FP32 from FP64 differences of the state (the rate added to
+ * the FP64 field as x + dt * rate), which removes most of the update's FP64
+ * work; the plain FP64 form and the per-routine entry points are always
+ * FP64.                                                                    */
 #define WPF_SOLVER_FP64_UPDATE 32
+/* WPF_SOLVER_NET_COARSE: in a solve whose learned correction was evaluated,
+ * also use the net's output w (computed on the half-resolution grid and
+ * prolongated) as a one-vector coarse space of the PCG: deflated PCG, whose
+ * start takes the coarse-grid correction w (w.r)/(w.A w) and whose search
+ * directions are kept A-orthogonal to w.  The solve ends at the same rtol;
+ * the error after k iterations is never above that of PCG without w.      */
+#define WPF_SOLVER_NET_COARSE 64
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

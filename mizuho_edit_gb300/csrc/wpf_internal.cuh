@@ -68,7 +68,10 @@ enum Slot {
     S_KLOG0, S_KLOG1,   // sum of log K_rock and of its square (input normalisation)
     S_KERR,             // set (int) by a kernel whose bounded wait ran out
     S_UPL0, S_UPL1,     // wpf_upload: one int per field whose values changed (4 ints)
-    S_COUNT = 32
+    S_WAW,              // e_net . A'e_net (the learned coarse space's 1x1 operator)
+    S_WR, S_WQ,         // e_net . r and e_net . q of the PCG with the learned coarse space
+    S_GAM,              // its coefficient e_net . r / e_net . A'e_net in this iteration
+    S_COUNT = 40
 };
 
 // Physics parameters in the form the kernels use.
@@ -247,7 +250,8 @@ struct wpf_handle {
     bool host_pageable_direct;   // kernels reach pageable host memory in place (host page tables)
     struct wpf_net* ws_net;  // learned warm start (not owned), or null
     const struct wpf_net* ws_net_warm;   // the net whose kernels ran once outside a capture
-    float* ws_e[2];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output)
+    float* ws_e[3];          // materialised starts: e_ext = a d1 + b d2, e_net (prolonged net output),
+                             // and A'e_net (the deflated PCG's coarse space)
     uint16_t* ws_in;         // net input (bf16, net grid, 16 channels)
     float* ws_out;           // net output channel 0 (net grid)
     float* ws_klog;          // net input channel 0, normalised log K_rock (net grid; K_rock is

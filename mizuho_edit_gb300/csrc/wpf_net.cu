@@ -1376,6 +1376,9 @@ int ws_net_correction(wpf_handle* h) {
     if (!h->ws_in && (rc = dev_alloc(h, (void**)&h->ws_in, sizeof(uint16_t) * nv * 16))) return rc;
     if (!h->ws_out && (rc = dev_alloc(h, (void**)&h->ws_out, sizeof(float) * nv))) return rc;
     if (!h->ws_e[1] && (rc = dev_alloc(h, (void**)&h->ws_e[1], sizeof(float) * g.total))) return rc;
+    if ((h->opts.flags & WPF_SOLVER_NET_COARSE) && !h->ws_e[2] &&
+        (rc = dev_alloc(h, (void**)&h->ws_e[2], sizeof(float) * g.total)))
+        return rc;
     if ((rc = ws_klog_prepare(h))) return rc;
     WPF_CUDA(cudaMemsetAsync(h->dsc + S_DPH2, 0, sizeof(double), s));
     WPF_LAUNCH(h, KC_OTHER, net::k_dphase_stats<<<row_blocks(h, g), RB, 0, s>>>(g, h->phase, h->phase_n, h->dsc));
@@ -1402,6 +1405,9 @@ int ws_net_prepare(wpf_handle* h) {
     if (!h->ws_in && (rc = dev_alloc(h, (void**)&h->ws_in, sizeof(uint16_t) * nv * 16))) return rc;
     if (!h->ws_out && (rc = dev_alloc(h, (void**)&h->ws_out, sizeof(float) * nv))) return rc;
     if (!h->ws_e[1] && (rc = dev_alloc(h, (void**)&h->ws_e[1], sizeof(float) * g.total))) return rc;
+    if ((h->opts.flags & WPF_SOLVER_NET_COARSE) && !h->ws_e[2] &&
+        (rc = dev_alloc(h, (void**)&h->ws_e[2], sizeof(float) * g.total)))
+        return rc;
     if ((rc = ws_klog_prepare(h))) return rc;
     if (h->ws_net_warm != h->ws_net) {
         if ((rc = wpf_net_forward(h->ws_net, h->ws_in, h->ws_out, (void*)s))) return rc;

@@ -189,20 +189,27 @@ def train(net: WarmStartNet, pairs, epochs: int, lr: float, seed: int = 0, val_f
     return {"train": hist, "val": vhist, "best_epoch": best[1] if best else -1}
 
 
-def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int, net_always: bool = False):
+def evaluate(case, net: WarmStartNet | None, steps: int, spinup: int, net_always: bool = False,
+             net_coarse: bool = False, step_graph: bool = False, fields: dict | None = None):
     """Per-step stats of a run with the extrapolated start, with or without
-    the network: (relres0, inner iterations, warm_start code) per timed step.
-    net_always evaluates the net at every solve instead of only where the
-    extrapolation misses the tolerance by at most 1.02x."""
+    the network: (relres0, inner iterations, warm_start code, relres) per
+    timed step.  net_always evaluates the net at every solve instead of only
+    where the extrapolation misses the tolerance by at most 1.02x; net_coarse
+    also uses its output as the PCG's one-vector coarse space; step_graph runs
+    the steps as one graph launch each.  fields (a dict) receives the final
+    phase, concentration and pressure."""
     out = []
     with Simulation(case.params, case.permeab_rock, case.phase, case.concent, solver="mixed",
-                    rtol=1e-8, extrapolate=True, net_always=net_always) as sim:
+                    rtol=1e-8, extrapolate=True, net_always=net_always, net_coarse=net_coarse,
+                    step_graph=step_graph) as sim:
         attach(sim, net)
         for _ in range(spinup):
             sim.step()
         for _ in range(steps):
             st = sim.step()
-            out.append((st.relres0, st.inner_iterations, st.warm_start))
+            out.append((st.relres0, st.inner_iterations, st.warm_start, st.relres))
+        if fields is not None:
+            fields.update(sim.download("phase", "concent", "pressure"))
         attach(sim, None)
     return out
 

@@ -5,7 +5,8 @@ and concentration (relative L2 over the halo arrays).
 * 64^3, 200 steps, log-K variance 1, correlation length 4 cells: the plain
   FP64 form, the FP32-refined form (1e-8 Darcy residual, extrapolated start,
   one graph launch per step) and the same with the learned start (its
-  correction evaluated at every solve).
+  correction evaluated at every solve), without and with its output as the
+  PCG's one-vector coarse space.
 * 128^3, 500 steps, log-K variance 2, correlation length 8 cells: the plain
   FP64 form against the FP32-refined form, both against the oracle.
 
@@ -41,6 +42,8 @@ def _forms(names):
         "mixed": dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True),
         # the net evaluated at every solve (not only inside its gate)
         "learned": dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True, net_always=True),
+        "learned_coarse": dict(solver="mixed", rtol=1e-8, extrapolate=True, step_graph=True, net_always=True,
+                               net_coarse=True),
     }
     return {k: forms[k] for k in names}
 
@@ -60,7 +63,7 @@ def _run(oracle_mod, n, log_var, corr_len, seed, steps, checks, names):
     try:
         for name, kw in _forms(names).items():
             sims[name] = Simulation(p, case.permeab_rock, case.phase, case.concent, **kw)
-            if name == "learned":
+            if name.startswith("learned"):
                 net = learned.WarmStartNet(n // 2, n // 2, n // 2)
                 net.set_params(learned.WarmStartNet.load_params(learned.DEFAULT_WEIGHTS))
                 learned.attach(sims[name], net)
@@ -73,7 +76,7 @@ def _run(oracle_mod, n, log_var, corr_len, seed, steps, checks, names):
             for name, sim in sims.items():
                 st = sim.step_unfused() if s in checks else sim.step()
                 assert st.converged, f"{name}: solve did not converge at step {s}"
-                net_kept += name == "learned" and st.warm_start == 2
+                net_kept += name.startswith("learned") and st.warm_start == 2
             if s in checks:
                 for name, sim in sims.items():
                     assert sim.dtime == pytest.approx(ref.dtime, rel=1e-9), name
@@ -84,8 +87,8 @@ def _run(oracle_mod, n, log_var, corr_len, seed, steps, checks, names):
                           f"u {e['velocity']:.2e} phi {e['phase']:.2e} c {e['concent']:.2e}")
         return errs, net_kept, ref.diagnostics(), {k: s.diagnostics() for k, s in sims.items()}
     finally:
-        for sim in sims.values():
-            if "learned" in sims and sim is sims["learned"]:
+        for name, sim in sims.items():
+            if name.startswith("learned"):
                 learned.attach(sim, None)
             sim.close()
         for net in nets:
@@ -102,8 +105,9 @@ def _check(errs, names, checks):
 
 def test_config_64cubed_200_steps(oracle_mod):
     """64^3, 200 steps (log-K variance 1, correlation 4 cells): FP64,
-    FP32-refined and learned forms against the oracle after 100 and 200 steps."""
-    names = ("fp64", "mixed", "learned")
+    FP32-refined and learned forms (start only, and start + coarse space)
+    against the oracle after 100 and 200 steps."""
+    names = ("fp64", "mixed", "learned", "learned_coarse")
     checks = (100, 200)
     errs, net_kept, rd, gd = _run(oracle_mod, 64, 1.0, 4.0, 2026, 200, checks, names)
     _check(errs, names, checks)
