@@ -579,12 +579,18 @@ def ensemble_pass(args):
     members = ensemble.make_members((16, 16, 16))
     tuned = ensemble.autotune(members, spinup=10, steps=4, log=lambda *a: None)
     res = ensemble.run(members, tuned, args.ensemble_steps, 20, 16, log=lambda *a: None)
+    # the same steps in the two other launch forms, for comparison
+    turn = ensemble.run(members, tuned, args.ensemble_steps, 20, 16, log=lambda *a: None, in_turn=True)
+    pool = ensemble.run(members, tuned, args.ensemble_steps, 20, 16, log=lambda *a: None, step_graph=False)
     return {"metric": "ensemble cell-updates/s", "value": res["ensemble_cell_updates_per_s"],
             "members": res["members"], "shapes": res["shapes"], "steps": res["steps"],
             "spinup": res["spinup"], "wall_s": res["wall_s"],
             "member_steps_per_s": res["member_steps_per_s"],
             "converged_last_step": res["converged_last_step"],
             "launch": "one CUDA graph launch per ensemble step (all members' steps as branches)",
+            "other_launch_forms": {
+                "members_in_turn_one_graph_launch_each": turn["ensemble_cell_updates_per_s"],
+                "host_driven_steps_16_threads": pool["ensemble_cell_updates_per_s"]},
             "tuned": ensemble.tuned_table(tuned)}
 
 

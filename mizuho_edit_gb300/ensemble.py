@@ -102,11 +102,14 @@ def autotune(members, spinup: int = 20, steps: int = 6, log=print):
     return best
 
 
-def run(members, tuned, steps: int, spinup: int, threads: int, log=print, step_graph: bool = True):
+def run(members, tuned, steps: int, spinup: int, threads: int, log=print, step_graph: bool = True,
+        in_turn: bool = False):
     """Advance every member `spinup` untimed steps, then `steps` timed ones
     through wpf_ensemble_run (step_graph: every step from the third one launch
     of one graph holding all members; else host-driven steps from a thread
-    pool); returns the throughput figures."""
+    pool); in_turn (with step_graph) times the members' steps one after
+    another instead, each wpf_step one launch of that member's own graph.
+    Returns the throughput figures."""
     import torch
     sims = [_sim(shape, kw, _opts(tuned[shape][0] if tuned else CANDIDATES[0]), step_graph)
             for shape, kw in members]
@@ -118,16 +121,31 @@ def run(members, tuned, steps: int, spinup: int, threads: int, log=print, step_g
         stats = (capi.StepStats * n)()
         status = (C.c_int32 * n)()
         ok = (capi.WPF_OK, capi.WPF_ERR_NOT_CONVERGED)
-        capi.check(L.wpf_ensemble_run(hs, n, 1, spinup, threads, dt, stats, status), "ensemble spin-up", ok)
+        warm = 2 if in_turn else 0   # the members' own graphs are captured in these
+        capi.check(L.wpf_ensemble_run(hs, n, 1, spinup - warm, threads, dt, stats, status), "ensemble spin-up",
+                   ok)
+
+        def in_turn_steps(first, count):
+            for it in range(first, first + count):
+                for m in range(n):
+                    d = C.c_double(dt[m])
+                    status[m] = L.wpf_step(hs[m], it, C.byref(d), C.byref(stats[m]))
+                    capi.check(status[m], "wpf_step", ok)
+                    dt[m] = d.value
+        if warm:
+            in_turn_steps(1 + spinup - warm, warm)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        capi.check(L.wpf_ensemble_run(hs, n, 1 + spinup, steps, threads, dt, stats, status), "ensemble", ok)
+        if in_turn:
+            in_turn_steps(1 + spinup, steps)
+        else:
+            capi.check(L.wpf_ensemble_run(hs, n, 1 + spinup, steps, threads, dt, stats, status), "ensemble", ok)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         cells = sum(int(np.prod(shape)) for shape, _ in members)
         res = {"members": n, "shapes": {str(s): sum(1 for m in members if m[0] == s) for s in SHAPES},
                "steps": steps, "spinup": spinup, "threads": threads, "wall_s": wall,
-               "one_graph_per_step": step_graph,
+               "one_graph_per_step": step_graph and not in_turn,
                "ensemble_cell_updates_per_s": cells * steps / wall,
                "member_steps_per_s": n * steps / wall,
                "converged_last_step": int(sum(1 for s in stats if s.converged)),
