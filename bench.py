@@ -407,6 +407,17 @@ def device_memory(arms):
     return {"library_bytes": int(nb.value), "in_use_bytes": int(total - free), "hbm_bytes": int(total)}
 
 
+def fp64_peak(arms):
+    """The device's FP64 FMA throughput (wpf_measure_fp64_rate): the ceiling of
+    the kernels bound by the FP64 pipe, which the measured copy and BF16 GEMM
+    peaks do not give."""
+    from mizuho_edit_gb300 import capi
+    t = C.c_double()
+    rc = arms.sim.L.wpf_measure_fp64_rate(C.byref(t))
+    return {"tflops": t.value if rc == capi.WPF_OK else None, "unit": "TFLOP/s",
+            "source": "wpf_measure_fp64_rate: 8 independent FP64 FMA chains per thread, 2048 threads per SM"}
+
+
 def roofline_window(args, arms):
     """The finest-level red-black sweep timed per launch (the step's largest
     HBM-bound share): its kernel class is timed with events around every
@@ -519,6 +530,7 @@ def run_ours(args):
     value = head_line["value"]
     roof, breakdown = roofline_window(args, arms)
     memory = device_memory(arms)
+    fp64 = fp64_peak(arms)
     out = {
         "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head_line["ms_per_step"],
@@ -539,6 +551,7 @@ def run_ours(args):
         "clocks": head_line.get("clocks"),
         "windows": windows,
         "device_memory": memory,
+        "fp64_peak": fp64,
     }
     last = windows[-1]
     if "plain_fp64" in last:

@@ -321,6 +321,13 @@ int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatc
  * class (finite / infinite / NaN) or sign. */
 int wpf_check_reciprocal(const double* host_values, int64_t n, int64_t* max_ulp, int64_t* mismatches);
 
+/* FP64 fused multiply-add throughput of the current device, in TFLOP/s
+ * (2 per FMA) in *tflops: eight independent FMA chains per thread, 2048
+ * threads on every SM, timed with CUDA events after one untimed run.  The
+ * ceiling of the kernels bound by the FP64 pipe (the outer FP64 residual,
+ * calcPermeability's harmonic means, the FP64 form's update).              */
+int wpf_measure_fp64_rate(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -306,6 +306,10 @@ module wpf_gb300
          integer(c_int64_t), value :: n
          integer(c_int64_t), intent(out) :: max_ulp, mismatches
       end function wpf_check_reciprocal
+      integer(c_int) function wpf_measure_fp64_rate(tflops) bind(C, name="wpf_measure_fp64_rate")
+         import :: c_int, c_double
+         real(c_double), intent(out) :: tflops
+      end function wpf_measure_fp64_rate
       ! ---- the learned start (wpf_net.h); device arrays as c_ptr
       integer(c_int) function wpf_net_create(nx, ny, nz, net) bind(C, name="wpf_net_create")
          import :: c_int, c_ptr, c_int32_t

@@ -125,6 +125,7 @@ SIGNATURES = {
                                    C.POINTER(StepStats), C.POINTER(C.c_int32)]),
     "wpf_check_conversions": (C.c_int, [DP, C.c_int64, C.POINTER(C.c_int64)]),
     "wpf_check_reciprocal": (C.c_int, [DP, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "wpf_measure_fp64_rate": (C.c_int, [DP]),
     # include/wpf_net.h: the learned warm start
     "wpf_net_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "wpf_net_destroy": (C.c_int, [C.c_void_p]),

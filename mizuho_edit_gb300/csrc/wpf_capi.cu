@@ -886,6 +886,61 @@ extern "C" int wpf_check_reciprocal(const double* host_values, int64_t n, int64_
     return rc;
 }
 
+// FP64 FMA throughput: eight independent chains per thread (a <- a b + c
+// converges to c / (1 - b), so the values stay finite); every thread stores
+// its sum so that no chain is dead code.
+__global__ void __launch_bounds__(256) k_fp64_rate(double* out, int iters, double b, double c) {
+    double a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = 1e-3 * threadIdx.x + q;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = fma(a[q], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += a[q];
+    out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" int wpf_measure_fp64_rate(double* tflops) {
+    using namespace wpf;
+    if (!tflops) return WPF_ERR_ARG;
+    *tflops = 0.0;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) {
+        cudaGetLastError();
+        return WPF_ERR_CUDA;
+    }
+    const unsigned blocks = (unsigned)nsm * 8u;   // 2048 threads per SM
+    const int iters = 4096;
+    double* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks * 256) != cudaSuccess) {
+        cudaGetLastError();
+        return WPF_ERR_NOMEM;
+    }
+    int rc = WPF_OK;
+    float ms = 0.f;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = WPF_ERR_CUDA;
+    if (!rc) {
+        k_fp64_rate<<<blocks, 256>>>(out, iters, 0.999999, 1e-6);   // untimed
+        cudaEventRecord(e0);
+        for (int r = 0; r < 3; ++r) k_fp64_rate<<<blocks, 256>>>(out, iters, 0.999999, 1e-6);
+        cudaEventRecord(e1);
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess ||
+            !(ms > 0.f))
+            rc = WPF_ERR_CUDA;
+    }
+    if (!rc) *tflops = 3.0 * 2.0 * 8.0 * iters * (double)blocks * 256.0 / (ms * 1e-3) / 1e12;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(out);
+    cudaGetLastError();
+    return rc;
+}
+
 extern "C" int wpf_check_conversions(const double* host_values, int64_t n, int64_t* mismatches) {
     using namespace wpf;
     if (!host_values || n < 0 || !mismatches) return WPF_ERR_ARG;

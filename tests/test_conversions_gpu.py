@@ -66,3 +66,18 @@ def test_newton_reciprocal_within_two_ulp():
                "wpf_check_reciprocal")
     assert bad.value == 0
     assert 0 <= ulp.value <= 2
+
+
+def test_fp64_rate():
+    """The FP64 FMA throughput probe returns a rate in the range a GB300 can
+    have (spec sheet ~1.25 TFLOP/s; the bound is loose on purpose), twice the
+    same to 10 %."""
+    import ctypes as C
+    from mizuho_edit_gb300 import capi
+    L = capi.load()
+    a, b = C.c_double(), C.c_double()
+    capi.check(L.wpf_measure_fp64_rate(C.byref(a)), "wpf_measure_fp64_rate")
+    capi.check(L.wpf_measure_fp64_rate(C.byref(b)), "wpf_measure_fp64_rate")
+    print(f"FP64 FMA rate: {a.value:.3f} and {b.value:.3f} TFLOP/s")
+    assert 0.2 < a.value < 20.0
+    assert abs(a.value - b.value) <= 0.1 * a.value
