@@ -138,6 +138,15 @@ typedef struct wpf_solver_opts {
  * directions are kept A-orthogonal to w.  The solve ends at the same rtol;
  * the error after k iterations is never above that of PCG without w.      */
 #define WPF_SOLVER_NET_COARSE 64
+/* WPF_SOLVER_FIXED_START: with WPF_SOLVER_EXTRAPOLATE, start from the
+ * quadratic-in-time extrapolation e = a d1 + b d2 of the last two increments
+ * with a, b fixed by the step sizes.  By default the FP32-refined form, when
+ * it holds the FP64 residual of the previous pressure under the new
+ * transmissibilities (its kept residual) and the last step's was below 100
+ * rtol, takes the a, b that minimise the residual ||r(p) - A (a d1 + b d2)||
+ * instead (never larger than the fixed choice's, which lies in the same
+ * span).                                                                   */
+#define WPF_SOLVER_FIXED_START 128
 
 /* Per-step / per-solve statistics. */
 typedef struct wpf_step_stats {

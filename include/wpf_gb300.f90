@@ -40,6 +40,7 @@ module wpf_gb300
    integer(c_int32_t), parameter :: WPF_SOLVER_NET_ALWAYS = 16
    integer(c_int32_t), parameter :: WPF_SOLVER_FP64_UPDATE = 32
    integer(c_int32_t), parameter :: WPF_SOLVER_NET_COARSE = 64
+   integer(c_int32_t), parameter :: WPF_SOLVER_FIXED_START = 128
    integer(c_int32_t), parameter :: WPF_NOALLOC_MAX_PLANES = 4096
    ! learned start (wpf_net.h)
    integer(c_int32_t), parameter :: WPF_NET_IN_CHANNELS = 16

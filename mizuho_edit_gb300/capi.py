@@ -31,6 +31,7 @@ SOLVER_STEP_GRAPH = 8
 SOLVER_NET_ALWAYS = 16
 SOLVER_FP64_UPDATE = 32
 SOLVER_NET_COARSE = 64
+SOLVER_FIXED_START = 128
 
 
 class WpfError(RuntimeError):

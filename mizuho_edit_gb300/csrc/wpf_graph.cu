@@ -165,6 +165,7 @@ __global__ void k_step_begin(StepCtl* c, double* dsc, double dt_c, double dt_a) 
         c->wa = (float)(hn / h1 + q / h1);
         c->wb = (float)(-q / h2);
     }
+    c->bnorm_prev = c->bnorm;   // the least-squares start's scale (k_ctl_ls_begin)
     c->bnorm = c->relres = c->relres0 = c->r0 = c->tol = 0.0;
     c->pass = c->outer = c->inner = c->it = c->need_pcg = c->accept = c->used = c->pcgs = c->net_runs = 0;
     c->alpha = 0.f;
@@ -296,6 +297,8 @@ int step_graph_finish(wpf_handle* h, const StepCounts& n, wpf_step_stats* st, do
     memcpy(&kerr, d + S_KERR, sizeof(int));
     const double taumin = dkey_inv(key);
     h->taumin_last = taumin;
+    h->ls_rp_rel = c.rp_rel;   // the least-squares start's record, for a host-driven next step
+    h->ls_bnorm = c.bnorm;
     h->last_active = nw[0] + nw[1];
     h->last_interface = nw[0];
     h->ws_hn = c.dt;
@@ -390,6 +393,8 @@ int step_graph_sync_ctl(wpf_handle* h) {
     if (!h->gctl_dirty) return WPF_OK;
     h->gctl_host->h1 = h->ws_h1;
     h->gctl_host->h2 = h->ws_h2;
+    h->gctl_host->rp_rel = h->ls_rp_rel;   // the host-driven solves' record for the least-squares start
+    h->gctl_host->bnorm = h->ls_bnorm;
     WPF_CUDA(cudaMemcpyAsync(h->gctl, h->gctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
     h->gctl_dirty = false;
     return WPF_OK;

@@ -71,6 +71,9 @@ enum Slot {
     S_WAW,              // e_net . A'e_net (the learned coarse space's 1x1 operator)
     S_WR, S_WQ,         // e_net . r and e_net . q of the PCG with the learned coarse space
     S_GAM,              // its coefficient e_net . r / e_net . A'e_net in this iteration
+    S_LS0,              // the least-squares start: r.A'd1, r.A'd2, |A'd1|^2, A'd1.A'd2, |A'd2|^2
+    S_LS4 = S_LS0 + 4,
+    S_LSSCALE,          // the power of two its dots scale r and A'd by
     S_COUNT = 40
 };
 
@@ -129,6 +132,10 @@ struct StepCtl {
     int status;              // WPF_OK / WPF_ERR_NOT_CONVERGED / WPF_ERR_NONFINITE
     int pcgs;                // PCG runs
     int net_runs;            // the learned correction was evaluated this step (0 / 1)
+    int ls;                  // the least-squares start is taken this step (0 / 1)
+    int ls_pad;
+    double rp_rel;           // ||r(p)|| / ||b|| of the last pass 0 (kept across steps)
+    double bnorm_prev;       // ||b|| of the last step (the least-squares dots' scale)
 };
 
 // Builds a CUDA graph from stream-captured segments and conditional nodes.
@@ -280,6 +287,8 @@ struct wpf_handle {
     bool bact_ok;
     int last_active;         // its length in the last step
     int last_interface;      // of which interface cells
+    double ls_rp_rel;        // host-driven solve: ||r(p)|| / ||b|| of the last pass 0
+    double ls_bnorm;         // and ||b|| of the last solve (the least-squares start's inputs)
     wpf::Phys* dphys;        // device copy of phys
     long long nlaunch;       // kernels launched on this handle so far
     // per-kernel-class event timers (enabled by wpf_set_kernel_timing)

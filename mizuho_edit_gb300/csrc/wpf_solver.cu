@@ -190,6 +190,86 @@ __device__ __forceinline__ R apply_l0(const R* __restrict__ cx, const R* __restr
             cz[n - sz] * from_f32<R>(e[n - sz]));
 }
 
+// The least-squares start (the default; WPF_SOLVER_FIXED_START keeps the
+// fixed coefficients): the five dots of min_{a,b} ||r - A'(a d1 + b d2)||, r
+// the kept FP64 residual of p under this step's transmissibilities, A' the
+// level-0 operator; A'd1 and A'd2 formed on the fly, one pass.  r and A'd are
+// scaled by a power of two s (from the last step's ||b||, so that they are
+// O(1) at the tolerance's scale) and the dots accumulated in FP32 per thread,
+// FP64 across threads; the solution does not depend on s.  Dirichlet cells
+// carry no residual.  c non-null (the step graph): a no-op unless c->ls.
+template <typename R>
+__global__ void __launch_bounds__(RB) k_ws_ls_dots(Grid g, const R* __restrict__ cx, const R* __restrict__ cy,
+                                                   const R* __restrict__ cz, const R* __restrict__ diag,
+                                                   const uint8_t* __restrict__ fl, const float* __restrict__ d1,
+                                                   const float* __restrict__ d2, const double* __restrict__ rk,
+                                                   const StepCtl* c, double scale, double* dsc) {
+    if (c && !c->ls) return;
+    const double s = c ? dsc[S_LSSCALE] : scale;
+    const float sf = (float)s;
+    const long long sy = g.P, sz = g.S;
+    float ra = 0.f, rb = 0.f, aa = 0.f, ab = 0.f, bb = 0.f;
+    ROW_LOOP(g) {
+        const long long n = g.at(i, j, k);
+        if (fl[n] & F_DIR) continue;
+        const float u = to_f32<R>(apply_l0(cx, cy, cz, diag, d1, n, sy, sz)) * sf;
+        const float v = to_f32<R>(apply_l0(cx, cy, cz, diag, d2, n, sy, sz)) * sf;
+        const float r = f64_to_f32(rk[n] * s);
+        ra = fmaf(r, u, ra);
+        rb = fmaf(r, v, rb);
+        aa = fmaf(u, u, aa);
+        ab = fmaf(u, v, ab);
+        bb = fmaf(v, v, bb);
+    }
+    block_add((double)ra, dsc + S_LS0);
+    block_add((double)rb, dsc + S_LS0 + 1);
+    block_add((double)aa, dsc + S_LS0 + 2);
+    block_add((double)ab, dsc + S_LS0 + 3);
+    block_add((double)bb, dsc + S_LS0 + 4);
+}
+
+// The 2x2 normal equations of the least-squares start; a one-direction fit
+// when d2 adds nothing to d1, and the given (a, b) kept when neither fits.
+__host__ __device__ inline void ws_ls_solve(const double* m, float* a, float* b) {
+    const double ra = m[0], rb = m[1], aa = m[2], ab = m[3], bb = m[4];
+    const double det = aa * bb - ab * ab;
+    if (aa > 0.0 && bb > 0.0 && det > 1e-6 * aa * bb && det == det && ra == ra && rb == rb) {
+        *a = (float)((ra * bb - rb * ab) / det);
+        *b = (float)((aa * rb - ab * ra) / det);
+    } else if (aa > 0.0 && ra == ra) {
+        *a = (float)(ra / aa);
+        *b = 0.f;
+    }
+}
+// Whether the least-squares start is taken this step: when the previous
+// pressure's residual under the new T (the last pass 0's record) is below
+// LS_WINDOW rtol.  Measured at 256^3 (time-steps/s, least-squares start
+// always / below 100 rtol / below 10 rtol): kwh 10^3 early in the run, p at
+// ~46 rtol, 329.5 / 329.4 / 292.1; late, p at ~1.7 rtol, 363.5 / 362.9 /
+// 355.2; kwh 20 early, p at ~390 rtol, 314.7 / 339.8 / 339.5 (the fit
+// costs its pass and saves no iteration there); kwh 20 late, p at ~30 rtol,
+// 336.6 / 336.6 / 264.4.  And the power of two that brings values of the
+// size rtol ||b|| / sqrt(cells) to ~1.
+constexpr double LS_WINDOW = 100.0;
+__host__ __device__ inline bool ws_ls_wanted(double rp_rel, double bnorm_prev, double rtol) {
+    return rp_rel > 0.0 && rp_rel < LS_WINDOW * rtol && bnorm_prev > 0.0;
+}
+__host__ __device__ inline double ws_ls_scale(double bnorm_prev, double rtol, long long cells) {
+    const double v = bnorm_prev * rtol / sqrt((double)(cells > 0 ? cells : 1));
+    int e = (v > 0.0 && v == v) ? ilogb(v) : 0;
+    e = e < -100 ? -100 : (e > 100 ? 100 : e);
+    return ldexp(1.0, -e);
+}
+__global__ void k_ctl_ls_begin(StepCtl* c, double* dsc, double rtol, long long cells) {
+    if (threadIdx.x) return;
+    c->ls = ws_ls_wanted(c->rp_rel, c->bnorm_prev, rtol) ? 1 : 0;
+    dsc[S_LSSCALE] = ws_ls_scale(c->bnorm_prev, rtol, cells);
+}
+__global__ void k_ctl_ws_ls(StepCtl* c, const double* dsc) {
+    if (threadIdx.x || !c->ls) return;
+    ws_ls_solve(dsc + S_LS0, &c->wa, &c->wb);
+}
+
 // Pass-0 residual of the start p + e_ext: r0 = r(p) in FP64 exactly as
 // k_resid64 (||r0||^2 into S_RR0WS, ||b_ref||^2 into S_BB64), then
 // r_ext = r0 - A'e_ext with A'e from the level-0 coefficients in precision R
@@ -1823,6 +1903,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     const float* e2 = nullptr;   // ... + alpha e_net
     float alpha = 0.f;
     const float* wc = nullptr;   // the learned coarse space of this solve's PCGs
+    bool ws_tried = false;       // pass 0 evaluated r(p) beside the extrapolated start
     bool ext_pending = false;    // a start accepted but not yet added to the pressure
     // the FP64 residual kept for the next solve (mixed form with the
     // extrapolated start): written by every plain pass, read by pass 0
@@ -1832,10 +1913,22 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         WPF_CUDA(cudaMemsetAsync(h->dsc + S_RR64, 0, 5 * sizeof(double), s));   // RR64 BB64 RR0WS RW WW
         bool plain = true;
         if (pass == 0 && ws_on && h->ws_hist > 0) {
+            ws_tried = true;
             float wa = 0.f, wb = 0.f;
             ws_coeffs(h, &wa, &wb);
-            if ((rc = ws_build_ext(h, wa, wb))) return rc;
             const double* rk_in = (rk && h->rkeep_ok) ? rk : nullptr;
+            if (rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START) &&
+                ws_ls_wanted(h->ls_rp_rel, h->ls_bnorm, h->opts.rtol)) {   // the least-squares start
+                WPF_CUDA(cudaMemsetAsync(h->dsc + S_LS0, 0, 5 * sizeof(double), s));
+                WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(
+                    g, H.lv[0].cx, H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->flags, h->ws[0],
+                    h->ws_hist >= 2 ? h->ws[1] : h->ws[0], rk_in, nullptr,
+                    ws_ls_scale(h->ls_bnorm, h->opts.rtol, (long long)g.nx * g.ny * g.nz), h->dsc));
+                WPF_CUDA(cudaGetLastError());
+                if ((rc = read_slot(h, S_LS0, 5))) return rc;
+                ws_ls_solve(h->hsc + S_LS0, &wa, &wb);
+            }
+            if ((rc = ws_build_ext(h, wa, wb))) return rc;
             auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
             WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
                 g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx, H.lv[0].cy,
@@ -1903,7 +1996,12 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         if (pass == 0) bnorm = sqrt(h->hsc[S_BB64]);
         const double rnorm = sqrt(h->hsc[S_RR64]);
         relres = bnorm > 0.0 ? rnorm / bnorm : rnorm;
-        if (pass == 0) relres0 = relres;
+        if (pass == 0) {
+            relres0 = relres;
+            // the next step's least-squares start: how close p itself was
+            h->ls_bnorm = bnorm;
+            h->ls_rp_rel = ws_tried && bnorm > 0.0 ? sqrt(h->hsc[S_RR0WS]) / bnorm : relres;
+        }
         if (!(relres == relres) || isinf(relres)) { status = WPF_ERR_NONFINITE; break; }
         if (relres <= h->opts.rtol) {
             // an extrapolated start whose (partly FP32-evaluated) residual
@@ -1988,6 +2086,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
 __global__ void k_ctl_accept(StepCtl* c, double* dsc) {
     if (threadIdx.x) return;
     const double rstart = dsc[S_RR64], r0 = dsc[S_RR0WS];
+    if (dsc[S_BB64] > 0.0) c->rp_rel = sqrt(r0 / dsc[S_BB64]);   // for the next step's least-squares start
     if (rstart <= r0 && rstart == rstart) {
         c->accept = 1;
         c->used = 1;
@@ -2016,6 +2115,7 @@ __global__ void k_ctl_accept_net(StepCtl* c, double* dsc) {
     if (threadIdx.x) return;
     double rstart = dsc[S_RR64];
     const double r0 = dsc[S_RR0WS], rw = dsc[S_RW], ww = dsc[S_WW];
+    if (dsc[S_BB64] > 0.0) c->rp_rel = sqrt(r0 / dsc[S_BB64]);
     float alpha = 0.f;
     if (ww > 0.0 && rw > 0.0 && rw == rw) {
         alpha = (float)(rw / ww);
@@ -2182,11 +2282,24 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     if ((rc = gb_fork(h))) return rc;
     build_coarse(h, H, h->cap_side);
     if (ws_on) {
-        if (h->ws_early) {   // built beside calcPermeability
+        const bool early = h->ws_early;
+        if (early) {   // built beside calcPermeability
             WPF_CUDA(cudaEventRecord(h->cap_ws_join, h->cap_ws));
             WPF_CUDA(cudaStreamWaitEvent(s, h->cap_ws_join, 0));
             h->ws_early = false;
-        } else {
+        }
+        if (rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START)) {
+            // the least-squares start: its coefficients need this step's
+            // kept residual and level-0 operator, so it is built after them
+            WPF_CUDA(cudaMemsetAsync(d + S_LS0, 0, 5 * sizeof(double), s));
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_ls_begin<<<1, 32, 0, s>>>(c, d, h->opts.rtol,
+                                                                     (long long)g.nx * g.ny * g.nz));
+            WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags,
+                                                                        h->ws[0], h->ws[1], rk_in, c, 0.0, d));
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_ws_ls<<<1, 32, 0, s>>>(c, d));
+            WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
+                                                                       d, &c->wa));
+        } else if (!early) {
             WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
                                                                        d, &c->wa));
         }
@@ -2304,6 +2417,9 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
 int ws_capture_early(wpf_handle* h, bool* launched) {
     *launched = false;
     if (!((h->opts.flags & WPF_SOLVER_EXTRAPOLATE) && h->ws[0] && h->ws_e[0] && h->cap_ws)) return WPF_OK;
+    // the least-squares start is built after calcPermeability (it needs the
+    // kept residual corrected for this step)
+    if (h->opts.mode == WPF_SOLVER_MIXED && h->rkeep_ok && !(h->opts.flags & WPF_SOLVER_FIXED_START)) return WPF_OK;
     const Grid& g = h->g;
     WPF_CUDA(cudaEventRecord(h->cap_ws_fork, h->stream));
     WPF_CUDA(cudaStreamWaitEvent(h->cap_ws, h->cap_ws_fork, 0));

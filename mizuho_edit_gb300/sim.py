@@ -37,7 +37,7 @@ class Simulation:
                  sweep_min_cells: int = 0, w_from_level: int = 0, graphs: bool = True,
                  extrapolate: bool = False, tma: bool = True, step_graph: bool = False,
                  sweep_zchunk: int = 0, row_blocks_per_sm: int = 0, net_always: bool = False,
-                 fp64_update: bool = False, net_coarse: bool = False):
+                 fp64_update: bool = False, net_coarse: bool = False, fixed_start: bool = False):
         self.L = capi.load()
         self.params = p = params
         if p.tfac is None:
@@ -57,7 +57,8 @@ class Simulation:
                         sweep_min_cells=sweep_min_cells, w_from_level=w_from_level,
                         graphs=graphs, extrapolate=extrapolate, tma=tma, step_graph=step_graph,
                         sweep_zchunk=sweep_zchunk, row_blocks_per_sm=row_blocks_per_sm,
-                        net_always=net_always, fp64_update=fp64_update, net_coarse=net_coarse)
+                        net_always=net_always, fp64_update=fp64_update, net_coarse=net_coarse,
+                        fixed_start=fixed_start)
         # initial fields exactly as loadConfig builds them (wPFAW3D.f90:464-496)
         sh = self.halo_shape
         kr = np.full(sh, p.init_permeab, order="F")
@@ -108,7 +109,7 @@ class Simulation:
                    sweep_min_cells: int = 0, w_from_level: int = 0, graphs: bool = True,
                    extrapolate: bool = False, tma: bool = True, step_graph: bool = False,
                    sweep_zchunk: int = 0, row_blocks_per_sm: int = 0, net_always: bool = False,
-                   fp64_update: bool = False, net_coarse: bool = False):
+                   fp64_update: bool = False, net_coarse: bool = False, fixed_start: bool = False):
         """Solver options (wpf_set_solver); graphs=False launches every
         preconditioner cycle kernel by kernel instead of replaying a CUDA graph;
         extrapolate=True starts each solve from the pressure extrapolated in
@@ -122,7 +123,9 @@ class Simulation:
         when the extrapolated start misses rtol by at most 1.02x; fp64_update
         keeps the mixed form's update rates in FP64; net_coarse makes the net's
         output, in the solves where it was evaluated, the one-vector coarse
-        space of a deflated PCG."""
+        space of a deflated PCG; fixed_start keeps the extrapolated start's
+        fixed quadratic-in-time coefficients instead of the least-squares
+        ones."""
         m = {"fp64": capi.SOLVER_FP64, "mixed": capi.SOLVER_MIXED}[mode]
         flags = (0 if graphs else capi.SOLVER_NO_GRAPHS) | \
             (capi.SOLVER_EXTRAPOLATE if extrapolate else 0) | \
@@ -130,7 +133,8 @@ class Simulation:
             (capi.SOLVER_STEP_GRAPH if step_graph else 0) | \
             (capi.SOLVER_NET_ALWAYS if net_always else 0) | \
             (capi.SOLVER_FP64_UPDATE if fp64_update else 0) | \
-            (capi.SOLVER_NET_COARSE if net_coarse else 0)
+            (capi.SOLVER_NET_COARSE if net_coarse else 0) | \
+            (capi.SOLVER_FIXED_START if fixed_start else 0)
         o = capi.SolverOpts(m, max_outer, max_inner, smooth_sweeps, rtol, inner_rtol,
                             sweep_min_cells, w_from_level, flags, sweep_zchunk, row_blocks_per_sm)
         capi.check(self.L.wpf_set_solver(self.h, C.byref(o)), "wpf_set_solver")

@@ -105,9 +105,10 @@ def test_net_coarse_space():
         fields[name] = {}
         runs[name] = learned.evaluate(case, net, 10, 20, net_always=True, fields=fields[name], **kw)
     net.close()
+    # (the coarse space is on in every solve whose net ran, whether or not the
+    # start took the net's correction)
     for name, st in runs.items():
         assert all(s[3] <= 1e-8 for s in st), name
-        assert any(s[2] == 2 for s in st), name
     d = rel_l2(fields["coarse"]["pressure"], fields["start"]["pressure"])
     assert 1e-13 < d < 1e-6
     for k in ("pressure", "phase", "concent"):
