@@ -71,10 +71,10 @@ enum Slot {
     S_WAW,              // e_net . A'e_net (the learned coarse space's 1x1 operator)
     S_WR, S_WQ,         // e_net . r and e_net . q of the PCG with the learned coarse space
     S_GAM,              // its coefficient e_net . r / e_net . A'e_net in this iteration
-    S_LS0,              // the least-squares start: r.A'd1, r.A'd2, |A'd1|^2, A'd1.A'd2, |A'd2|^2
-    S_LS4 = S_LS0 + 4,
+    S_LS0,              // the least-squares start: r.A'd1, r.A'd2, |A'd1|^2, A'd1.A'd2, |A'd2|^2,
+    S_LS5 = S_LS0 + 5,  // |r|^2 (r = r(p), scaled)
     S_LSSCALE,          // the power of two its dots scale r and A'd by
-    S_COUNT = 40
+    S_COUNT = 48
 };
 
 // Physics parameters in the form the kernels use.
@@ -133,7 +133,7 @@ struct StepCtl {
     int pcgs;                // PCG runs
     int net_runs;            // the learned correction was evaluated this step (0 / 1)
     int ls;                  // the least-squares start is taken this step (0 / 1)
-    int ls_pad;
+    int ls_skip;             // its predicted residual meets rtol: pass 0's residual kernel is skipped
     double rp_rel;           // ||r(p)|| / ||b|| of the last pass 0 (kept across steps)
     double bnorm_prev;       // ||b|| of the last step (the least-squares dots' scale)
 };
@@ -607,7 +607,8 @@ void solver_drop_graphs(wpf_handle* h);   // after an options change
 int solve_pressure(wpf_handle* h, wpf_step_stats* st);
 // extrapolated / learned start (wpf_solver.cu, wpf_net.cu)
 void ws_coeffs(const wpf_handle* h, float* a, float* b);
-int ws_build_ext(wpf_handle* h, float a, float b);      // ws_e[0] = a d1 + b d2, S_WSS2 = sum d1^2
+int ws_build_ext(wpf_handle* h, float a, float b,      // ws_e[0] = a d1 + b d2, S_WSS2 = sum d1^2;
+                 float* dnew = nullptr);               // dnew: a copy of it there too
 int ws_net_correction(wpf_handle* h);                   // ws_e[1] from the attached net
 
 int ensure_per_routine_arrays(wpf_handle* h);

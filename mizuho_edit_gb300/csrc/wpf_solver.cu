@@ -157,10 +157,12 @@ __global__ void __launch_bounds__(RB) k_add_correction(Grid g, double* __restric
 // where every increment is zero); accumulates sum d1^2 and sum (d1 - d2)^2
 // (the scales the learned start works in) into S_WSS2 and S_WSD2.  With ab
 // non-null the coefficients are read from the device (ab[0], ab[1]).
+// dnew non-null: also e there (the increment record of an accepted start,
+// which pass 0's residual kernel writes when it runs)
 __global__ void __launch_bounds__(RB) k_ws_build_ext(Grid g, const float* __restrict__ d1,
                                                      const float* __restrict__ d2, float a, float b,
                                                      float* __restrict__ e, double* dsc,
-                                                     const float* ab = nullptr) {
+                                                     const float* ab = nullptr, float* __restrict__ dnew = nullptr) {
     if (ab) {
         a = ab[0];
         b = ab[1];
@@ -171,7 +173,9 @@ __global__ void __launch_bounds__(RB) k_ws_build_ext(Grid g, const float* __rest
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         const float v1 = d1[n], v2 = d2[n];
-        e[n] = __fmaf_rn(a, v1, __fmul_rn(b, v2));
+        const float ev = __fmaf_rn(a, v1, __fmul_rn(b, v2));
+        e[n] = ev;
+        if (dnew) dnew[n] = ev;
         s2 = __fmaf_rn(v1, v1, s2);
         const float dd = v1 - v2;
         q2 = __fmaf_rn(dd, dd, q2);
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(RB) k_ws_ls_dots(Grid g, const R* __restrict__
     const double s = c ? dsc[S_LSSCALE] : scale;
     const float sf = (float)s;
     const long long sy = g.P, sz = g.S;
-    float ra = 0.f, rb = 0.f, aa = 0.f, ab = 0.f, bb = 0.f;
+    float ra = 0.f, rb = 0.f, aa = 0.f, ab = 0.f, bb = 0.f, rr = 0.f;
     ROW_LOOP(g) {
         const long long n = g.at(i, j, k);
         if (fl[n] & F_DIR) continue;
@@ -220,12 +224,14 @@ __global__ void __launch_bounds__(RB) k_ws_ls_dots(Grid g, const R* __restrict__
         aa = fmaf(u, u, aa);
         ab = fmaf(u, v, ab);
         bb = fmaf(v, v, bb);
+        rr = fmaf(r, r, rr);
     }
     block_add((double)ra, dsc + S_LS0);
     block_add((double)rb, dsc + S_LS0 + 1);
     block_add((double)aa, dsc + S_LS0 + 2);
     block_add((double)ab, dsc + S_LS0 + 3);
     block_add((double)bb, dsc + S_LS0 + 4);
+    block_add((double)rr, dsc + S_LS0 + 5);
 }
 
 // The 2x2 normal equations of the least-squares start; a one-direction fit
@@ -241,6 +247,15 @@ __host__ __device__ inline void ws_ls_solve(const double* m, float* a, float* b)
         *b = 0.f;
     }
 }
+// ||r(p) - A'(a d1 + b d2)||^2 from the dots (scaled like them)
+__host__ __device__ inline double ws_ls_predict(const double* m, double a, double b) {
+    return m[5] - 2.0 * (a * m[0] + b * m[1]) + a * a * m[2] + 2.0 * a * b * m[3] + b * b * m[4];
+}
+// The predicted start residual at or below LS_SKIP rtol ||b|| (with the last
+// step's ||b||) skips pass 0's residual kernel: the start is accepted on the
+// prediction and the plain FP64 verification pass decides as always.
+constexpr double LS_SKIP = 0.8;
+
 // Whether the least-squares start is taken this step: when the previous
 // pressure's residual under the new T (the last pass 0's record) is below
 // LS_WINDOW rtol.  Measured at 256^3 (time-steps/s, least-squares start
@@ -263,11 +278,21 @@ __host__ __device__ inline double ws_ls_scale(double bnorm_prev, double rtol, lo
 __global__ void k_ctl_ls_begin(StepCtl* c, double* dsc, double rtol, long long cells) {
     if (threadIdx.x) return;
     c->ls = ws_ls_wanted(c->rp_rel, c->bnorm_prev, rtol) ? 1 : 0;
+    c->ls_skip = 0;
     dsc[S_LSSCALE] = ws_ls_scale(c->bnorm_prev, rtol, cells);
 }
-__global__ void k_ctl_ws_ls(StepCtl* c, const double* dsc) {
+// (rtol < 0: never skip)
+__global__ void k_ctl_ws_ls(StepCtl* c, double* dsc, double rtol) {
     if (threadIdx.x || !c->ls) return;
     ws_ls_solve(dsc + S_LS0, &c->wa, &c->wb);
+    const double s = dsc[S_LSSCALE], bn = c->bnorm_prev;
+    const double pred = fmax(ws_ls_predict(dsc + S_LS0, c->wa, c->wb), 0.0) / (s * s);
+    if (sqrt(pred) <= LS_SKIP * rtol * bn) {   // the norms pass 0 would have given
+        c->ls_skip = 1;
+        dsc[S_RR64] = pred;
+        dsc[S_RR0WS] = dsc[S_LS5] / (s * s);
+        dsc[S_BB64] = bn * bn;
+    }
 }
 
 // Pass-0 residual of the start p + e_ext: r0 = r(p) in FP64 exactly as
@@ -294,7 +319,9 @@ __global__ void __launch_bounds__(RB) k_resid64_ws(Grid g, const double* __restr
                                                    const R* __restrict__ diag,
                                                    const float* __restrict__ e1,
                                                    R* __restrict__ rout, float* __restrict__ dnew,
-                                                   double* dsc, const double* __restrict__ rk_in = nullptr) {
+                                                   double* dsc, const double* __restrict__ rk_in = nullptr,
+                                                   const int* skip = nullptr) {
+    if (skip && *skip) return;   // the least-squares start's prediction stands in (k_ctl_ws_ls)
     double rr1 = 0.0, rr0 = 0.0, bb = 0.0;
     R rr1r = 0;   // the same sum in R (with D)
     float rr0f = 0.f;               // ||r(p)||^2 in FP32 on the kept path (only the fallback test reads it)
@@ -1871,7 +1898,7 @@ void ws_coeffs(const wpf_handle* h, float* a, float* b) {
     *b = (float)(-c / h2);
 }
 
-int ws_build_ext(wpf_handle* h, float a, float b) {
+int ws_build_ext(wpf_handle* h, float a, float b, float* dnew) {
     const Grid& g = h->g;
     if (!h->ws_e[0]) {
         int rc = dev_alloc(h, (void**)&h->ws_e[0], sizeof(float) * g.total);
@@ -1879,7 +1906,7 @@ int ws_build_ext(wpf_handle* h, float a, float b) {
     }
     WPF_CUDA(cudaMemsetAsync(h->dsc + S_WSS2, 0, 2 * sizeof(double), h->stream));   // WSS2, WSD2
     WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<row_blocks(h, g), RB, 0, h->stream>>>(
-        g, h->ws[0], h->ws[1], a, b, h->ws_e[0], h->dsc));
+        g, h->ws[0], h->ws[1], a, b, h->ws_e[0], h->dsc, nullptr, dnew));
     WPF_CUDA(cudaGetLastError());
     return WPF_OK;
 }
@@ -1917,25 +1944,37 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             float wa = 0.f, wb = 0.f;
             ws_coeffs(h, &wa, &wb);
             const double* rk_in = (rk && h->rkeep_ok) ? rk : nullptr;
+            bool skip0 = false;   // pass 0's residual kernel replaced by the prediction
             if (rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START) &&
                 ws_ls_wanted(h->ls_rp_rel, h->ls_bnorm, h->opts.rtol)) {   // the least-squares start
-                WPF_CUDA(cudaMemsetAsync(h->dsc + S_LS0, 0, 5 * sizeof(double), s));
+                const double sc = ws_ls_scale(h->ls_bnorm, h->opts.rtol, (long long)g.nx * g.ny * g.nz);
+                WPF_CUDA(cudaMemsetAsync(h->dsc + S_LS0, 0, 6 * sizeof(double), s));
                 WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(
                     g, H.lv[0].cx, H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->flags, h->ws[0],
-                    h->ws_hist >= 2 ? h->ws[1] : h->ws[0], rk_in, nullptr,
-                    ws_ls_scale(h->ls_bnorm, h->opts.rtol, (long long)g.nx * g.ny * g.nz), h->dsc));
+                    h->ws_hist >= 2 ? h->ws[1] : h->ws[0], rk_in, nullptr, sc, h->dsc));
                 WPF_CUDA(cudaGetLastError());
-                if ((rc = read_slot(h, S_LS0, 5))) return rc;
+                if ((rc = read_slot(h, S_LS0, 6))) return rc;
                 ws_ls_solve(h->hsc + S_LS0, &wa, &wb);
+                const double pred = fmax(ws_ls_predict(h->hsc + S_LS0, wa, wb), 0.0) / (sc * sc);
+                // (the net, when it runs at every solve, needs pass 0's FP32 residual)
+                if (!(h->opts.flags & WPF_SOLVER_NET_ALWAYS) &&
+                    sqrt(pred) <= LS_SKIP * h->opts.rtol * h->ls_bnorm) {
+                    skip0 = true;
+                    h->hsc[S_RR64] = pred;
+                    h->hsc[S_RR0WS] = h->hsc[S_LS5] / (sc * sc);
+                    h->hsc[S_BB64] = h->ls_bnorm * h->ls_bnorm;
+                }
             }
-            if ((rc = ws_build_ext(h, wa, wb))) return rc;
-            auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
-            WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
-                g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx, H.lv[0].cy,
-                H.lv[0].cz, H.lv[0].diag, h->ws_e[0], H.r, dnew, h->dsc, rk_in));
-            WPF_CUDA(cudaGetLastError());
-            rc = read_slot(h, S_RR64, 5);
-            if (rc) return rc;
+            if ((rc = ws_build_ext(h, wa, wb, skip0 ? dnew : nullptr))) return rc;
+            if (!skip0) {
+                auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
+                WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
+                    g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx,
+                    H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->ws_e[0], H.r, dnew, h->dsc, rk_in, nullptr));
+                WPF_CUDA(cudaGetLastError());
+                rc = read_slot(h, S_RR64, 5);
+                if (rc) return rc;
+            }
             double rstart = h->hsc[S_RR64];
             const double r0 = h->hsc[S_RR0WS];
             double rw = 0.0, ww = 0.0;
@@ -1985,21 +2024,23 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         }
         if (plain) {
             if (pass == 0 && ws_on) WPF_CUDA(cudaMemsetAsync(dnew, 0, sizeof(float) * g.total, s));
+            // ||b|| on every plain pass: after a pass 0 whose residual the
+            // least-squares prediction replaced, the verification pass gives it
             WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                              h->flags, h->qterm, resid_dsum(h), H.r, h->dsc, pass == 0,
+                                                              h->flags, h->qterm, resid_dsum(h), H.r, h->dsc, 1,
                                                               nullptr, nullptr, rk));
             WPF_CUDA(cudaGetLastError());
             h->rkeep_ok = rk != nullptr;
             rc = read_slot(h, S_RR64, 2);
             if (rc) return rc;
         }
-        if (pass == 0) bnorm = sqrt(h->hsc[S_BB64]);
+        if (pass == 0 || h->hsc[S_BB64] > 0.0) bnorm = sqrt(h->hsc[S_BB64]);
         const double rnorm = sqrt(h->hsc[S_RR64]);
         relres = bnorm > 0.0 ? rnorm / bnorm : rnorm;
+        h->ls_bnorm = bnorm;   // the next step's least-squares start: its scale
         if (pass == 0) {
             relres0 = relres;
-            // the next step's least-squares start: how close p itself was
-            h->ls_bnorm = bnorm;
+            // and how close p itself was
             h->ls_rp_rel = ws_tried && bnorm > 0.0 ? sqrt(h->hsc[S_RR0WS]) / bnorm : relres;
         }
         if (!(relres == relres) || isinf(relres)) { status = WPF_ERR_NONFINITE; break; }
@@ -2161,7 +2202,10 @@ __global__ void k_ctl_pass(StepCtl* c, const double* dsc, double rtol, double in
     const int pass = c->pass;
     int cont = 0, pcg = 0;
     if (c->status != WPF_ERR_NONFINITE) {   // else a PCG of the last pass broke down
-        if (pass == 0) c->bnorm = sqrt(dsc[S_BB64]);
+        // ||b|| from pass 0, and again from every plain pass (after a pass 0
+        // whose residual the least-squares prediction replaced, the
+        // verification pass gives the exact one)
+        if (pass == 0 || dsc[S_BB64] > 0.0) c->bnorm = sqrt(dsc[S_BB64]);
         const double bnorm = c->bnorm;
         const double rnorm = sqrt(dsc[S_RR64]);
         const double relres = bnorm > 0.0 ? rnorm / bnorm : rnorm;
@@ -2291,22 +2335,25 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
         if (rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START)) {
             // the least-squares start: its coefficients need this step's
             // kept residual and level-0 operator, so it is built after them
-            WPF_CUDA(cudaMemsetAsync(d + S_LS0, 0, 5 * sizeof(double), s));
+            WPF_CUDA(cudaMemsetAsync(d + S_LS0, 0, 6 * sizeof(double), s));
             WPF_LAUNCH(h, KC_OTHER, k_ctl_ls_begin<<<1, 32, 0, s>>>(c, d, h->opts.rtol,
                                                                      (long long)g.nx * g.ny * g.nz));
             WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags,
                                                                         h->ws[0], h->ws[1], rk_in, c, 0.0, d));
-            WPF_LAUNCH(h, KC_OTHER, k_ctl_ws_ls<<<1, 32, 0, s>>>(c, d));
+            // (the net, when it runs at every solve, needs pass 0's FP32 residual)
+            WPF_LAUNCH(h, KC_OTHER, k_ctl_ws_ls<<<1, 32, 0, s>>>(
+                c, d, (h->opts.flags & WPF_SOLVER_NET_ALWAYS) ? -1.0 : h->opts.rtol));
             WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
-                                                                       d, &c->wa));
+                                                                       d, &c->wa, dnew));
         } else if (!early) {
             WPF_LAUNCH(h, KC_RESID64, k_ws_build_ext<<<rb, RB, 0, s>>>(g, h->ws[0], h->ws[1], 0.f, 0.f, h->ws_e[0],
                                                                        d, &c->wa));
         }
         auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
+        const bool lsq = rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START);
         WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
             g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
-            h->ws_e[0], H.r, dnew, d, rk_in));
+            h->ws_e[0], H.r, dnew, d, rk_in, lsq ? &c->ls_skip : nullptr));
         if (net) {
             // the learned correction in an IF node, taken when the extrapolated
             // start misses rtol by at most NET_WINDOW (k_ctl_net_gate); the
@@ -2393,7 +2440,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
                                                                     net ? h->ws_e[1] : nullptr, dnew, c));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_advance<<<1, 32, 0, s>>>(c, d));
     WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                               h->flags, h->qterm, resid_dsum(h), H.r, d, 0,
+                                                               h->flags, h->qterm, resid_dsum(h), H.r, d, 1,
                                                                nullptr, nullptr, rk));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
                                                          mixed, h_pass));
