@@ -421,7 +421,8 @@ __device__ __forceinline__ double resid_face_delta(double* rk, const uint8_t* __
     return d;
 }
 
-__global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
+constexpr int PB_X = 32, PB_Y = 4, PB_Z = 2;   // k_permeability's block
+__global__ void __launch_bounds__(PB_X * PB_Y * PB_Z) k_permeability(Grid g, Phys P, const double* __restrict__ ph,
                                const double* __restrict__ prev, const double* __restrict__ kr,
                                double* __restrict__ Tx, double* __restrict__ Ty,
                                double* __restrict__ Tz, double* __restrict__ Kx,
@@ -430,34 +431,56 @@ __global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
                                const double* __restrict__ pr = nullptr, uint8_t* __restrict__ mark = nullptr,
                                double* __restrict__ Tvx = nullptr, double* __restrict__ Tvy = nullptr,
                                double* __restrict__ Tvz = nullptr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    const long long n = g.at(i, j, k);
+    // A block of PB_X x PB_Y x PB_Z face-cells; the cell permeabilities its
+    // faces need (its cells and the +x/+y/+z neighbours) are computed once
+    // each into shared memory instead of once per adjacent face.
+    constexpr int KX = PB_X + 1, KY = PB_Y + 1, KZ = PB_Z + 1, KN = KX * KY * KZ;
+    __shared__ double sK[KN];
+    __shared__ unsigned char need[KN];
+    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+    const int tid = tx + PB_X * (ty + PB_Y * tz);
+    const int i0 = blockIdx.x * PB_X, j0 = blockIdx.y * PB_Y, k0 = blockIdx.z * PB_Z;
+    const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
+    for (int q = tid; q < KN; q += PB_X * PB_Y * PB_Z) need[q] = 0;
+    __syncthreads();
+    const bool in = i <= g.nx && j <= g.ny && k <= g.nz;
+    const long long n = in ? g.at(i, j, k) : 0;
     // with prev: a face is recomputed only when one of its two cells changed
     // phase (the harmonic means are FP64 divisions, the costliest work here)
-    bool fx = true, fy = true, fz = true;
-    if (prev) {
+    bool fx = in, fy = in, fz = in;
+    if (in && prev) {
         const bool c0 = bits(ph[n]) != bits(prev[n]);
         fx = c0 || bits(ph[n + 1]) != bits(prev[n + 1]);
         fy = c0 || bits(ph[n + g.P]) != bits(prev[n + g.P]);
         fz = c0 || bits(ph[n + g.S]) != bits(prev[n + g.S]);
-        if (!(fx || fy || fz)) return;
     }
-    auto K0 = [&](long long m) {
+    const int t0 = tx + KX * (ty + KY * tz);   // this face-cell in the K tile
+    if (fx || fy || fz) {
+        need[t0] = 1;
+        if (fx) need[t0 + 1] = 1;
+        if (fy) need[t0 + KX] = 1;
+        if (fz) need[t0 + KX * KY] = 1;
+    }
+    if (!__syncthreads_or(fx || fy || fz)) return;   // block-uniform
+    for (int q = tid; q < KN; q += PB_X * PB_Y * PB_Z) {
+        if (!need[q]) continue;
+        const int qx = q % KX, qy = (q / KX) % KY, qz = q / (KX * KY);
+        const long long m = g.at(i0 + qx, j0 + qy, k0 + qz);
         const double f = 0.5 * (1.0 + ph[m]);
-        return P.kwh * f + kr[m] * (1.0 - f);
-    };
-    const double a = K0(n);
+        sK[q] = P.kwh * f + kr[m] * (1.0 - f);   // K0 of :567-574
+    }
+    __syncthreads();
+    if (!(fx || fy || fz)) return;   // no barrier below
+    const double a = sK[t0];
     const double a2 = 2.0 * a;   // 2 a b = (2 a) b exactly: one multiply per face
     const bool in_j = j >= 1 && j <= g.ny, in_k = k >= 1 && k <= g.nz, in_i = i >= 1 && i <= g.nx;
     const double p_a = rk ? pr[n] : 0.0;
     double own = 0.0;
-    // face towards m (owner n): T = 2 a b / (a + b) / mu, 0 outside `inside`
-    auto face = [&](long long m, bool inside, double* __restrict__ T, double* __restrict__ Kf,
+    // face towards m (owner n; its K0 at tile offset dm): T = 2 a b / (a + b)
+    // / mu, 0 outside `inside`
+    auto face = [&](long long m, int dm, bool inside, double* __restrict__ T, double* __restrict__ Kf,
                     double* __restrict__ Tv) {
-        const double b = K0(m);
+        const double b = sK[t0 + dm];
         const double kf = (a2 * b) * rcp_nr(a + b);
         const double t = inside ? kf * inv_mu : 0.0;
         if (rk) own += resid_face_delta(rk, fl, pr, n, m, p_a, t - T[n]);
@@ -469,9 +492,9 @@ __global__ void k_permeability(Grid g, Phys P, const double* __restrict__ ph,
         }
         if (Kf) Kf[n] = kf;
     };
-    if (fx) face(n + 1, i >= 1 && i < g.nx && in_j && in_k, Tx, Kx, Tvx);
-    if (fy) face(n + g.P, j >= 1 && j < g.ny && in_i && in_k, Ty, Ky, Tvy);
-    if (fz) face(n + g.S, k >= 1 && k < g.nz && in_i && in_j, Tz, Kz, Tvz);
+    if (fx) face(n + 1, 1, i >= 1 && i < g.nx && in_j && in_k, Tx, Kx, Tvx);
+    if (fy) face(n + g.P, KX, j >= 1 && j < g.ny && in_i && in_k, Ty, Ky, Tvy);
+    if (fz) face(n + g.S, KX * KY, k >= 1 && k < g.nz && in_i && in_j, Tz, Kz, Tvz);
     // boundary faces stay 0 (dT = 0): only interior pairs change the residual
     if (rk && own != 0.0 && !(fl[n] & F_DIR)) atomicAdd(rk + n, own);
 }
@@ -952,7 +975,7 @@ static double inv_mu(const wpf_handle* h) { return 1.0 / h->prm.viscosity; }
 
 int phys_permeability(wpf_handle* h, bool materialise) {
     const Grid& g = h->g;
-    dim3 b = cell_block(), gr = cell_grid(g.nx + 1, g.ny + 1, g.nz + 1);
+    const dim3 b = cell_block();
     if (materialise) {
         int rc = ensure_per_routine_arrays(h);
         if (rc) return rc;
@@ -967,7 +990,9 @@ int phys_permeability(wpf_handle* h, bool materialise) {
     h->rkeep_ok = keep;
     // every face recomputed: the level-0 operator is rebuilt whole next time
     if (!prev) h->l0_inc_ok = false;
-    WPF_LAUNCH(h, KC_PERM, k_permeability<<<gr, b, 0, h->stream>>>(
+    const dim3 pb(PB_X, PB_Y, PB_Z);
+    const dim3 pg((g.nx + 1 + PB_X - 1) / PB_X, (g.ny + 1 + PB_Y - 1) / PB_Y, (g.nz + 1 + PB_Z - 1) / PB_Z);
+    WPF_LAUNCH(h, KC_PERM, k_permeability<<<pg, pb, 0, h->stream>>>(
         g, h->phys, h->phase, prev, h->krock, h->T[0], h->T[1], h->T[2],
         materialise ? h->Kf[0] : nullptr, materialise ? h->Kf[1] : nullptr,
         materialise ? h->Kf[2] : nullptr, inv_mu(h), keep ? h->rkeep : nullptr, h->flags, h->pressure,
