@@ -93,12 +93,15 @@ __global__ void __launch_bounds__(RB) k_resid64(Grid g, const double* __restrict
                                                 R* __restrict__ rout, double* dsc, int want_b,
                                                 const int* skip = nullptr,
                                                 float* __restrict__ zero_out = nullptr,
-                                                double* __restrict__ rk_out = nullptr) {
+                                                double* __restrict__ rk_out = nullptr,
+                                                const int* want_b_dev = nullptr) {
     // skip: a device flag that, when set, makes the launch a no-op (the
     // device-resident step launches this pass unconditionally); zero_out: a
     // field whose interior is cleared on the way; rk_out: the residual kept
-    // in FP64 for the next solve's pass 0
+    // in FP64 for the next solve's pass 0; want_b_dev: a device flag that
+    // also asks for ||b|| (set when pass 0's residual was a prediction)
     if (skip && *skip) return;
+    if (want_b_dev && *want_b_dev) want_b = 1;
     double rr = 0.0, bb = 0.0;
     R rrr = 0;
     const long long sy = g.P, sz = g.S;
@@ -1931,6 +1934,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
     float alpha = 0.f;
     const float* wc = nullptr;   // the learned coarse space of this solve's PCGs
     bool ws_tried = false;       // pass 0 evaluated r(p) beside the extrapolated start
+    bool b_predicted = false;    // pass 0 took ||b|| from the last solve (least-squares prediction)
     bool ext_pending = false;    // a start accepted but not yet added to the pressure
     // the FP64 residual kept for the next solve (mixed form with the
     // extrapolated start): written by every plain pass, read by pass 0
@@ -1960,6 +1964,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
                 if (!(h->opts.flags & WPF_SOLVER_NET_ALWAYS) &&
                     sqrt(pred) <= LS_SKIP * h->opts.rtol * h->ls_bnorm) {
                     skip0 = true;
+                    b_predicted = true;
                     h->hsc[S_RR64] = pred;
                     h->hsc[S_RR0WS] = h->hsc[S_LS5] / (sc * sc);
                     h->hsc[S_BB64] = h->ls_bnorm * h->ls_bnorm;
@@ -2024,11 +2029,11 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
         }
         if (plain) {
             if (pass == 0 && ws_on) WPF_CUDA(cudaMemsetAsync(dnew, 0, sizeof(float) * g.total, s));
-            // ||b|| on every plain pass: after a pass 0 whose residual the
-            // least-squares prediction replaced, the verification pass gives it
+            // ||b|| on pass 0, and on the passes after a pass 0 whose residual
+            // the least-squares prediction replaced (its ||b|| was the last step's)
             WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                              h->flags, h->qterm, resid_dsum(h), H.r, h->dsc, 1,
-                                                              nullptr, nullptr, rk));
+                                                              h->flags, h->qterm, resid_dsum(h), H.r, h->dsc,
+                                                              pass == 0 || b_predicted, nullptr, nullptr, rk));
             WPF_CUDA(cudaGetLastError());
             h->rkeep_ok = rk != nullptr;
             rc = read_slot(h, S_RR64, 2);
@@ -2202,9 +2207,8 @@ __global__ void k_ctl_pass(StepCtl* c, const double* dsc, double rtol, double in
     const int pass = c->pass;
     int cont = 0, pcg = 0;
     if (c->status != WPF_ERR_NONFINITE) {   // else a PCG of the last pass broke down
-        // ||b|| from pass 0, and again from every plain pass (after a pass 0
-        // whose residual the least-squares prediction replaced, the
-        // verification pass gives the exact one)
+        // ||b|| from pass 0, and from the verification pass after a pass 0
+        // whose residual the least-squares prediction replaced (the exact one)
         if (pass == 0 || dsc[S_BB64] > 0.0) c->bnorm = sqrt(dsc[S_BB64]);
         const double bnorm = c->bnorm;
         const double rnorm = sqrt(dsc[S_RR64]);
@@ -2439,9 +2443,11 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
                                                                     ws_on ? h->ws_e[0] : nullptr,
                                                                     net ? h->ws_e[1] : nullptr, dnew, c));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_advance<<<1, 32, 0, s>>>(c, d));
+    // ||b|| again only after a pass 0 whose residual the least-squares
+    // prediction replaced (its ||b|| was the last step's)
     WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
-                                                               h->flags, h->qterm, resid_dsum(h), H.r, d, 1,
-                                                               nullptr, nullptr, rk));
+                                                               h->flags, h->qterm, resid_dsum(h), H.r, d, 0,
+                                                               nullptr, nullptr, rk, &c->ls_skip));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
                                                          mixed, h_pass));
     WPF_CUDA(cudaGetLastError());
