@@ -232,9 +232,11 @@ def config_of(args, world):
     n = args.n
     w = windows_of(args)
     arm = headline_arm(args)
-    start = {"learned": "time-extrapolated pressure plus the learned network's correction "
-                        "(fallback to the previous pressure when it does not lower the FP64 residual)",
-             "extrapolated": "time-extrapolated pressure (fallback to the previous pressure)"}[arm]
+    ext = ("previous pressure plus the least-squares combination of the last two increments "
+           "(the quadratic-in-time extrapolation where the previous pressure is above 100 rtol)")
+    start = {"learned": ext + " plus the learned network's correction where its gate opens "
+                        "(fallback to the previous pressure when the start does not lower the FP64 residual)",
+             "extrapolated": ext + " (fallback to the previous pressure)"}[arm]
     return {"workload": workload_name(args), "grid": [n, n, n],
             "solver": "fp32-mg-pcg-in-fp64-refinement", "darcy_rtol": args.rtol, "dtype_state": "f64",
             "warm_start": start, "form": arm,

@@ -113,8 +113,10 @@ class Simulation:
         """Solver options (wpf_set_solver); graphs=False launches every
         preconditioner cycle kernel by kernel instead of replaying a CUDA graph;
         extrapolate=True starts each solve from the pressure extrapolated in
-        time (with the fallback to the previous pressure); tma=False stages the
-        pipelined sweep with cp.async instead of bulk-tensor copies;
+        time -- in the mixed form the least-squares combination of the last two
+        increments unless fixed_start -- with the fallback to the previous
+        pressure; tma=False stages the pipelined sweep with cp.async instead of
+        bulk-tensor copies;
         step_graph=True runs each step (from the fourth) as one CUDA graph launch
         with the solver's loops on the device; sweep_zchunk and row_blocks_per_sm
         are launch shapes (z planes per block of the pipelined sweep, blocks per
