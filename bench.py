@@ -409,6 +409,27 @@ def device_memory(arms):
     return {"library_bytes": int(nb.value), "in_use_bytes": int(total - free), "hbm_bytes": int(total)}
 
 
+def update_roofline(head_line, ncell):
+    """The fused update (classification + listed cells), the largest share of
+    a late-window step once the least-squares start has taken the PCG out of
+    most steps.  Algorithmic bytes per step: the classification reads phase
+    and concentration of every cell (16 B) and writes both for the copied
+    cells (16 B); a listed cell also reads pressure (8 B), the three face
+    factors Tv (24 B), its flags (1 B) and its work-list index (4 B) and
+    writes both fields (16 B).  Timed per step by the step's own events."""
+    peak, peak_kind = measured_peaks()
+    listed = head_line["update_active_fraction"] * ncell
+    nbytes = 16.0 * ncell + 16.0 * (ncell - listed) + 53.0 * listed
+    ms = head_line["fused_update_ms"]
+    achieved = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else None
+    return {"kernel": "fused update (k_update_split + k_update_active)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "bytes_per_step": nbytes,
+            "ms_per_step": ms, "peak_source": peak_kind,
+            "note": "latency- and FP64-pipe-bound, not HBM-bound (ncu at a late 160^3 state: "
+                    "DRAM 14 % of peak, FP64 pipe 55 %, profiles/k_update_active_160_late.md)"}
+
+
 def fp64_peak(arms):
     """The device's FP64 FMA throughput (wpf_measure_fp64_rate): the ceiling of
     the kernels bound by the FP64 pipe, which the measured copy and BF16 GEMM
@@ -550,6 +571,7 @@ def run_ours(args):
         "update_interface_fraction": head_line["update_interface_fraction"],
         "gpu_launches": head_line["gpu_launches"],
         "roofline": roof,
+        "roofline_update": update_roofline(head_line, ncell),
         "clocks": head_line.get("clocks"),
         "windows": windows,
         "device_memory": memory,
