@@ -8,6 +8,8 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "wpf_internal.cuh"
@@ -87,6 +89,23 @@ int ensure_per_routine_arrays(wpf_handle* h) {
         if (rc) return rc;
     }
     return WPF_OK;
+}
+
+int resident_blocks(const void* f, int threads, size_t smem, int cap) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, int>> seen;   // (kernel, blocks per SM) for RB-thread launches
+    const bool cacheable = threads == RB && smem == 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (cacheable)
+        for (const auto& e : seen)
+            if (e.first == f) return e.second < cap ? e.second : cap;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, smem) != cudaSuccess || b < 1) {
+        cudaGetLastError();
+        return cap;
+    }
+    if (cacheable) seen.emplace_back(f, b);
+    return b < cap ? b : cap;
 }
 
 }  // namespace wpf

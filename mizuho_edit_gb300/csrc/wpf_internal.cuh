@@ -582,6 +582,23 @@ inline unsigned row_blocks(const wpf_handle* h, const Grid& g, int per_sm = 0) {
     return (unsigned)(patches < cap ? patches : cap);
 }
 
+// Blocks of `threads` threads (and `smem` dynamic shared bytes) of kernel f
+// that one SM holds at once, at most cap (cap when the query fails); cached
+// per kernel.  A grid-stride kernel launched with more blocks per SM than fit
+// runs the rest as a second, partial wave: with 8 per SM where 5 fit, the
+// last 3 start when the first 5 end, and the pass takes two block lifetimes
+// instead of 8/5 of one.
+int resident_blocks(const void* f, int threads, size_t smem, int cap);
+
+// row_blocks for the row-patch kernel f: as many blocks per SM as stay
+// resident (at most 8), unless the caller set row_blocks_per_sm.
+template <typename F>
+inline unsigned row_blocks_for(const wpf_handle* h, const Grid& g, F f) {
+    const int per_sm = h->opts.row_blocks_per_sm > 0 ? h->opts.row_blocks_per_sm
+                                                     : resident_blocks((const void*)f, RB, 0, 8);
+    return row_blocks(h, g, per_sm);
+}
+
 template <typename T>
 __device__ __forceinline__ void block_add(T v, double* acc) {
     __shared__ T sm_add[32];

@@ -1781,7 +1781,7 @@ static int pcg(wpf_handle* h, Hierarchy<R>& H, double tol, int maxit, int nu, in
             WPF_LAUNCH(h, KC_OTHER, k_cc_mu<<<1, 32, 0, s>>>(nullptr, d));
         }
         WPF_CUDA(cudaMemsetAsync(d + S_PQ, 0, 2 * sizeof(double), s));   // S_PQ, S_RR
-        WPF_LAUNCH(h, KC_APPLY, k_apply_p<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.z, pold, pnew,
+        WPF_LAUNCH(h, KC_APPLY, k_apply_p<R><<<row_blocks_for(h, g, k_apply_p<R>), RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.z, pold, pnew,
                                                  H.q, d + S_RZ0 + cur, d + S_RZ0 + (cur ^ 1),
                                                  it == 0, nullptr, d + S_PQ, wc, d + S_GAM));
         WPF_LAUNCH(h, KC_VEC, k_update_xr<R><<<rb, RB, 0, s>>>(g, H.x, H.r, pnew, pnew, H.q, d + S_RZ0 + cur,
@@ -1953,7 +1953,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
                 ws_ls_wanted(h->ls_rp_rel, h->ls_bnorm, h->opts.rtol)) {   // the least-squares start
                 const double sc = ws_ls_scale(h->ls_bnorm, h->opts.rtol, (long long)g.nx * g.ny * g.nz);
                 WPF_CUDA(cudaMemsetAsync(h->dsc + S_LS0, 0, 6 * sizeof(double), s));
-                WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(
+                WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<row_blocks_for(h, g, k_ws_ls_dots<R>), RB, 0, s>>>(
                     g, H.lv[0].cx, H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->flags, h->ws[0],
                     h->ws_hist >= 2 ? h->ws[1] : h->ws[0], rk_in, nullptr, sc, h->dsc));
                 WPF_CUDA(cudaGetLastError());
@@ -1973,7 +1973,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             if ((rc = ws_build_ext(h, wa, wb, skip0 ? dnew : nullptr))) return rc;
             if (!skip0) {
                 auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
-                WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
+                WPF_LAUNCH(h, KC_RESID64, kern<<<row_blocks_for(h, g, kern), RB, 0, s>>>(
                     g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), H.lv[0].cx,
                     H.lv[0].cy, H.lv[0].cz, H.lv[0].diag, h->ws_e[0], H.r, dnew, h->dsc, rk_in, nullptr));
                 WPF_CUDA(cudaGetLastError());
@@ -2031,7 +2031,7 @@ static int solve_impl(wpf_handle* h, Hierarchy<R>& H, wpf_step_stats* st) {
             if (pass == 0 && ws_on) WPF_CUDA(cudaMemsetAsync(dnew, 0, sizeof(float) * g.total, s));
             // ||b|| on pass 0, and on the passes after a pass 0 whose residual
             // the least-squares prediction replaced (its ||b|| was the last step's)
-            WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+            WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<row_blocks_for(h, g, k_resid64<R>), RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                               h->flags, h->qterm, resid_dsum(h), H.r, h->dsc,
                                                               pass == 0 || b_predicted, nullptr, nullptr, rk));
             WPF_CUDA(cudaGetLastError());
@@ -2342,7 +2342,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
             WPF_CUDA(cudaMemsetAsync(d + S_LS0, 0, 6 * sizeof(double), s));
             WPF_LAUNCH(h, KC_OTHER, k_ctl_ls_begin<<<1, 32, 0, s>>>(c, d, h->opts.rtol,
                                                                      (long long)g.nx * g.ny * g.nz));
-            WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags,
+            WPF_LAUNCH(h, KC_RESID64, k_ws_ls_dots<R><<<row_blocks_for(h, g, k_ws_ls_dots<R>), RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, h->flags,
                                                                         h->ws[0], h->ws[1], rk_in, c, 0.0, d));
             // (the net, when it runs at every solve, needs pass 0's FP32 residual)
             WPF_LAUNCH(h, KC_OTHER, k_ctl_ws_ls<<<1, 32, 0, s>>>(
@@ -2355,7 +2355,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
         }
         auto* kern = rk_in ? k_resid64_ws<R, true> : k_resid64_ws<R, false>;
         const bool lsq = rk_in && !(h->opts.flags & WPF_SOLVER_FIXED_START);
-        WPF_LAUNCH(h, KC_RESID64, kern<<<rb, RB, 0, s>>>(
+        WPF_LAUNCH(h, KC_RESID64, kern<<<row_blocks_for(h, g, kern), RB, 0, s>>>(
             g, h->pressure, h->T[0], h->T[1], h->T[2], h->flags, h->qterm, resid_dsum(h), L0.cx, L0.cy, L0.cz, L0.diag,
             h->ws_e[0], H.r, dnew, d, rk_in, lsq ? &c->ls_skip : nullptr));
         if (net) {
@@ -2388,11 +2388,11 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
         } else {
             WPF_LAUNCH(h, KC_OTHER, k_ctl_accept<<<1, 32, 0, s>>>(c, d));
         }
-        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<row_blocks_for(h, g, k_resid64<R>), RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                                    h->flags, h->qterm, resid_dsum(h), H.r, d, 1, &c->accept,
                                                                    dnew, rk));
     } else {
-        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+        WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<row_blocks_for(h, g, k_resid64<R>), RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                                    h->flags, h->qterm, resid_dsum(h), H.r, d, 1,
                                                                    nullptr, nullptr, rk));
     }
@@ -2428,7 +2428,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
         WPF_LAUNCH(h, KC_OTHER, k_cc_mu<<<1, 32, 0, s>>>(c, d));
     }
     WPF_CUDA(cudaMemsetAsync(d + S_PQ, 0, 2 * sizeof(double), s));   // PQ, RR
-    WPF_LAUNCH(h, KC_APPLY, k_apply_p<R><<<rb, RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.z, H.p2, H.p, H.q,
+    WPF_LAUNCH(h, KC_APPLY, k_apply_p<R><<<row_blocks_for(h, g, k_apply_p<R>), RB, 0, s>>>(g, L0.cx, L0.cy, L0.cz, L0.diag, H.z, H.p2, H.p, H.q,
                                                              d + S_RZ1, d + S_RZ0, 0, &c->it, d + S_PQ, wc,
                                                              d + S_GAM));
     WPF_LAUNCH(h, KC_VEC, k_update_xr<R><<<rb, RB, 0, s>>>(g, H.x, H.r, H.p, H.p2, H.q, d + S_RZ1, d + S_PQ, 0,
@@ -2445,7 +2445,7 @@ static int solve_capture_impl(wpf_handle* h, Hierarchy<R>& H, GraphBuilder& b, S
     WPF_LAUNCH(h, KC_OTHER, k_ctl_advance<<<1, 32, 0, s>>>(c, d));
     // ||b|| again only after a pass 0 whose residual the least-squares
     // prediction replaced (its ||b|| was the last step's)
-    WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<rb, RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
+    WPF_LAUNCH(h, KC_RESID64, k_resid64<R><<<row_blocks_for(h, g, k_resid64<R>), RB, 0, s>>>(g, h->pressure, h->T[0], h->T[1], h->T[2],
                                                                h->flags, h->qterm, resid_dsum(h), H.r, d, 0,
                                                                nullptr, nullptr, rk, &c->ls_skip));
     WPF_LAUNCH(h, KC_OTHER, k_ctl_pass<<<1, 32, 0, s>>>(c, d, h->opts.rtol, h->opts.inner_rtol, h->opts.max_outer,
