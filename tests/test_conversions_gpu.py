@@ -64,6 +64,7 @@ def test_newton_reciprocal_within_two_ulp():
     bad = C.c_int64(-1)
     capi.check(L.wpf_check_reciprocal(v.ctypes.data_as(capi.DP), v.size, C.byref(ulp), C.byref(bad)),
                "wpf_check_reciprocal")
+    print(f"refined reciprocal: largest distance from the IEEE 1/x {ulp.value} ulp over {v.size} values")
     assert bad.value == 0
     assert 0 <= ulp.value <= 2
 

