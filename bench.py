@@ -12,8 +12,9 @@ state: the learned start (the headline, `value`), the extrapolated start
 without the network, and the plain FP64 MG-PCG from the previous pressure.
 The headline is the last window, where the acid has reached almost every
 cell and the fused update works on the whole grid.  A second run at kwh = 20
-is reported beside it.  Inputs (FP64 fields and solver levels, ~3.5 GB) are
-far larger than the 129 MB L2, so no flush is needed between steps.
+is reported beside it.  Inputs (the FP64 fields a step reads are over 1 GB
+at 256^3; 5.8 GB of fields and solver levels in all) are far larger than the
+129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -253,7 +254,8 @@ def config_of(args, world):
             "step": "one CUDA graph launch per step" if not args.no_step_graph else "host-driven",
             "learned_correction": "evaluated in the step graph (an IF node) when the extrapolated "
                                   "start misses the 1e-8 tolerance by at most 1.02x (the net's measured reach)",
-            "l2_policy": "inputs larger than L2 (~3.5 GB of fields and solver levels per step)",
+            "l2_policy": "inputs larger than L2 (over 1 GB of FP64 fields read per step at 256^3; "
+                         "5.8 GB of fields and solver levels in all)",
             "parallelism": f"replicas{world}" if world > 1 else "single-domain"}
 
 
